@@ -1,0 +1,117 @@
+"""ctypes binding of the C ABI in ``include/gratopy_gb300.h``.
+
+Loads the in-tree ``gratopy_gb300/_build/libgratopy_gb300.so``.  There is no
+fallback: if the library is missing the import of any compute entry point
+raises, so a GPU run can never silently take another path.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libgratopy_gb300.so"
+
+GR_F32, GR_F64 = 0, 1
+GR_ORDER_F, GR_ORDER_C = 0, 1
+GR_RADON, GR_FANBEAM = 0, 1
+GR_OK = 0
+SC_SOLD, SC_ALPHA, SC_BETA, SC_DSQ, SC_FSQ, SC_RES, SC_SUM = range(7)
+SC_COUNT = 8
+
+
+class GrGeometry(ctypes.Structure):
+    """Mirror of ``struct gr_geometry``."""
+
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("dtype", ctypes.c_int),
+        ("Nx", ctypes.c_int),
+        ("Ny", ctypes.c_int),
+        ("Ns", ctypes.c_int),
+        ("Na", ctypes.c_int),
+        ("ofs", ctypes.c_void_p),
+        ("sdpd", ctypes.c_void_p),
+        ("geo", ctypes.c_double * 11),
+    ]
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_F = ctypes.c_float
+_D = ctypes.c_double
+_Z = ctypes.c_size_t
+_G = ctypes.POINTER(GrGeometry)
+
+# name -> (restype, argtypes); must match include/gratopy_gb300.h
+SIGNATURES = {
+    "gr_error_string": (ctypes.c_char_p, [_I]),
+    "gr_last_cuda_error": (_I, []),
+    "gr_version": (_I, []),
+    "gr_radon_fwd": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "gr_radon_bwd": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "gr_fan_fwd": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "gr_fan_bwd": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "gr_forward": (_I, [_G, _P, _P, _I, _I, _I, _P]),
+    "gr_backward": (_I, [_G, _P, _P, _I, _I, _I, _P]),
+    "gr_forward_residual": (_I, [_G, _P, _P, _P, _I, _I, _P]),
+    "gr_backward_axpy": (_I, [_G, _P, _P, _D, _I, _I, _P]),
+    "gr_forward_lambda": (_I, [_G, _P, _P, _P, _F, _F, _I, _I, _P]),
+    "gr_backward_tv_primal": (_I, [_G, _P, _P, _P, _P, _F, _F, _F, _I, _I, _P]),
+    "gr_forward_wsq": (_I, [_G, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "gr_backward_cg": (_I, [_G, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "gr_backward_sum": (_I, [_G, _P, _P, _P, _I, _I, _P]),
+    "gr_forward_partials": (_Z, [_G, _I]),
+    "gr_backward_partials": (_Z, [_G, _I, _I]),
+    "gr_weight_sinogram": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "gr_equ_mul_add": (_I, [_P, _D, _P, _I, _Z, _P]),
+    "gr_mul_add_add": (_I, [_P, _D, _P, _P, _I, _Z, _P]),
+    "gr_dot_partials_count": (_Z, []),
+    "gr_dot_partials": (_I, [_P, _P, _P, _I, _Z, _P]),
+    "gr_sum_partials": (_I, [_P, _P, _Z, _P]),
+    "gr_sum_values_partials": (_I, [_P, _P, _I, _Z, _P]),
+    "gr_tv_dual": (_I, [_P, _P, _F, _F, _I, _I, _I, _I, _I, _P]),
+    "gr_cg_alpha": (_I, [_P, _P, _Z, _D, _I, _P, _P]),
+    "gr_cg_update_d": (_I, [_P, _P, _P, _P, _I, _Z, _P, _P]),
+    "gr_cg_beta": (_I, [_P, _P, _Z, _P, _Z, _D, _I, _P, _P]),
+    "gr_cg_update_p": (_I, [_P, _P, _P, _I, _Z, _P, _P]),
+    "gr_scale_by_sum": (_I, [_P, _P, _I, _Z, _P]),
+}
+
+_lib = None
+
+
+class GratopyCudaError(RuntimeError):
+    """A C-ABI call returned an error code."""
+
+
+def load():
+    """Load the extension (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(
+                f"gratopy_gb300 CUDA extension not built ({LIB_PATH} missing); "
+                "run `python -m gratopy_gb300.build` (or __graft_entry__.build())"
+            )
+        lib = ctypes.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def call(name: str, *args) -> None:
+    """Call a status-returning entry point and raise on a nonzero code."""
+    rc = getattr(load(), name)(*args)
+    if rc != GR_OK:
+        lib = load()
+        msg = lib.gr_error_string(rc).decode()
+        cuda = lib.gr_last_cuda_error()
+        raise GratopyCudaError(f"{name} failed: {msg} (code {rc}, cudaError {cuda})")
+
+
+def raw(name: str):
+    return getattr(load(), name)

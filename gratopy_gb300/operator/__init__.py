@@ -1,0 +1,6 @@
+"""Operator API: algebra of projection operators (gratopy/operator/__init__.py)."""
+
+from .base import IDENTITY, ZERO, Operator, OperatorArithmeticOperation
+from .projection import Fanbeam, Radon
+
+__all__ = ["IDENTITY", "ZERO", "Operator", "OperatorArithmeticOperation", "Radon", "Fanbeam"]

@@ -1,0 +1,180 @@
+/*
+ * gratopy_gb300 -- C ABI of the GB300 (sm_103a) projection and
+ * reconstruction kernels.
+ *
+ * Conventions
+ *  - Every pointer argument named like an array (sino, img, ofs, ...) is a
+ *    DEVICE pointer owned by the caller; scalars and `const double* geo`
+ *    are host values.  Nothing here allocates or frees memory.
+ *  - `stream` is a cudaStream_t passed as void*; every call is
+ *    asynchronous on it and returns 0 (GR_OK) or an error code; nothing
+ *    throws across the ABI.  gr_error_string() names a code.
+ *  - dtype: GR_F32 or GR_F64.  order: GR_ORDER_F (x / detector fastest) or
+ *    GR_ORDER_C (z fastest), as in gratopy's pos_img_f / pos_img_c
+ *    (gratopy radon.cl:28-31).  Images are (Nx, Ny, Nz), sinograms
+ *    (Ns, Na, Nz); Nz = 1 for 2-D data.
+ *  - Per-angle table `ofs`: 8 reals per angle, angle-major (gratopy's
+ *    ofs_dict arrays in Fortran order); `sdpd`: Ns reals (fan beam only).
+ *    gratopy builds them in radon_struct (gratopy.py:380-578) and
+ *    fanbeam_struct (gratopy.py:706-1003).
+ */
+#ifndef GRATOPY_GB300_H
+#define GRATOPY_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define GR_API __attribute__((visibility("default")))
+#else
+#define GR_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { GR_F32 = 0, GR_F64 = 1 };
+enum { GR_ORDER_F = 0, GR_ORDER_C = 1 };
+enum { GR_RADON = 0, GR_FANBEAM = 1 };
+
+enum {
+  GR_OK = 0,
+  GR_ERR_ARG = 1,      /* null pointer, bad dtype/order/kind */
+  GR_ERR_SHAPE = 2,    /* sizes inconsistent with the geometry */
+  GR_ERR_CUDA = 3,     /* a CUDA launch or runtime call failed */
+  GR_ERR_TOO_BIG = 4   /* size beyond a documented limit */
+};
+
+/* Geometry of one projection problem.  geo[] holds gratopy's
+ * Geometryinformation vector in float64:
+ *   Radon (6):  [delta_x, delta_s, Nx, Ny, Ns, Na]           (gratopy.py:556-560)
+ *   Fan  (11):  [R, RE, ds/dx, x_mid, y_mid, s_mid, Nx, Ny, Ns, Na, delta_x]
+ *                                                          (gratopy.py:970-986) */
+typedef struct gr_geometry {
+  int kind;          /* GR_RADON | GR_FANBEAM */
+  int dtype;         /* GR_F32 | GR_F64: precision of ofs/sdpd and of the data */
+  int Nx, Ny, Ns, Na;
+  const void* ofs;   /* device: 8*Na reals */
+  const void* sdpd;  /* device: Ns reals (fan) or NULL (Radon) */
+  double geo[11];
+} gr_geometry;
+
+GR_API const char* gr_error_string(int code);
+/* Last CUDA error seen by this library on the calling thread (cudaError_t). */
+GR_API int gr_last_cuda_error(void);
+GR_API int gr_version(void);
+
+/* ---- The four projection kernels, argument order as gratopy's kernels ----
+ * radon.cl:66-161    radon_{T}_{so}{io}(sino, img, ofs, Geometryinformation) */
+GR_API int gr_radon_fwd(void* sino, const void* img, const void* ofs, const double* geo,
+                 int dtype, int Ns, int Na, int Nz, int sino_order, int img_order,
+                 void* stream);
+/* radon.cl:183-241   radon_ad_{T}_{io}{so}(img, sino, ofs, Geometryinformation) */
+GR_API int gr_radon_bwd(void* img, const void* sino, const void* ofs, const double* geo,
+                 int dtype, int Nx, int Ny, int Nz, int img_order, int sino_order,
+                 void* stream);
+/* fanbeam.cl:72-256  fanbeam_{T}_{so}{io}(sino, img, ofs, sdpd, Geometryinformation) */
+GR_API int gr_fan_fwd(void* sino, const void* img, const void* ofs, const void* sdpd,
+               const double* geo, int dtype, int Ns, int Na, int Nz, int sino_order,
+               int img_order, void* stream);
+/* fanbeam.cl:290-391 fanbeam_ad_{T}_{io}{so}(img, sino, ofs, sdpd, Geometryinformation) */
+GR_API int gr_fan_bwd(void* img, const void* sino, const void* ofs, const void* sdpd,
+               const double* geo, int dtype, int Nx, int Ny, int Nz, int img_order,
+               int sino_order, void* stream);
+
+/* ---- Geometry-generic projections (dispatch on g->kind) ----
+ * gratopy.py:1655-1685 (ProjectionSettings.forwardprojection/backprojection) */
+GR_API int gr_forward(const gr_geometry* g, void* sino, const void* img, int Nz, int sino_order,
+               int img_order, void* stream);
+GR_API int gr_backward(const gr_geometry* g, void* img, const void* sino, int Nz, int img_order,
+                int sino_order, void* stream);
+
+/* ---- Projections with a fused solver epilogue (image and sinogram share
+ * one order) ----
+ * Landweber (gratopy.py:2432-2444): r = A u - f  and  u += a * A^T r */
+GR_API int gr_forward_residual(const gr_geometry* g, void* r, const void* u, const void* f, int Nz,
+                        int order, void* stream);
+GR_API int gr_backward_axpy(const gr_geometry* g, void* u, const void* r, double a, int Nz, int order,
+                     void* stream);
+/* TV data dual step (total_variation.cl:95-106 on A u):
+ * lambda = (lambda + sigma (A u - f)) * mu2 */
+GR_API int gr_forward_lambda(const gr_geometry* g, void* lambda, const void* u, const void* f,
+                      float sigma, float mu2, int Nz, int order, void* stream);
+/* TV primal step (total_variation.cl:108-148 + gratopy.py:2708-2717 on A^T lambda):
+ * u_new = max(0, u + tau (div v - norming A^T lambda)); ubar = 2 u_new - u; u = u_new */
+GR_API int gr_backward_tv_primal(const gr_geometry* g, void* u, void* ubar, const void* v,
+                          const void* lambda, float tau, float norming, float z_distance,
+                          int Nz, int order, void* stream);
+/* CG (gratopy.py:2521-2542): q = A p with block partials of <W q, q>;
+ * snew = A^T d, x += alpha p with block partials of <snew, snew>.
+ * `skip` (device int, may be NULL) makes the launch a no-op when nonzero. */
+GR_API int gr_forward_wsq(const gr_geometry* g, void* q, const void* p, const void* w,
+                   double* partials, const int* skip, int Nz, int order, void* stream);
+GR_API int gr_backward_cg(const gr_geometry* g, void* snew, const void* d, void* x, const void* p,
+                   const double* alpha, double* partials, const int* skip, int Nz, int order,
+                   void* stream);
+/* normest (gratopy.py:2366-2376): img = A^T sino with block partials of sum(img). */
+GR_API int gr_backward_sum(const gr_geometry* g, void* img, const void* sino, double* partials,
+                    int Nz, int order, void* stream);
+/* Number of block partials the reducing launches above write. */
+GR_API size_t gr_forward_partials(const gr_geometry* g, int Nz);
+GR_API size_t gr_backward_partials(const gr_geometry* g, int Nz, int order);
+
+/* ---- Elementwise and reduction kernels ---- */
+/* utilities.cl:38-67 multiply/divide: out = sino * w[a]  (or / w[a]) */
+GR_API int gr_weight_sinogram(void* out, const void* sino, const void* w, int dtype, int Ns, int Na,
+                       int Nz, int order, int divide, void* stream);
+/* utilities.cl:69-73 equ_mul_add: rhs += a x */
+GR_API int gr_equ_mul_add(void* rhs, double a, const void* x, int dtype, size_t n, void* stream);
+/* utilities.cl:75-80 mul_add_add: rhs = a x + y */
+GR_API int gr_mul_add_add(void* rhs, double a, const void* x, const void* y, int dtype, size_t n,
+                   void* stream);
+/* Deterministic float64 dot product <a, b> (b may equal a), two stages:
+ * gr_dot_partials writes gr_dot_partials_count() block partials, then
+ * gr_sum_partials adds n partials in a fixed order into *out (device). */
+GR_API size_t gr_dot_partials_count(void);
+GR_API int gr_dot_partials(double* partials, const void* a, const void* b, int dtype, size_t n,
+                    void* stream);
+GR_API int gr_sum_partials(double* out, const double* partials, size_t n, void* stream);
+/* Plain sum of n reals (normest's clarray.sum), same two-stage scheme. */
+GR_API int gr_sum_values_partials(double* partials, const void* a, int dtype, size_t n, void* stream);
+
+/* ---- TV dual step (total_variation.cl:54-93 + :150-167 fused):
+ * v = P_{|.|<=1}(v + sigma grad(ubar)); v holds 4 reals per pixel. */
+GR_API int gr_tv_dual(void* v, const void* ubar, float sigma, float z_distance, int dtype, int Nx,
+               int Ny, int Nz, int order, void* stream);
+
+/* ---- Device-resident solver scalars ----
+ * sc is a device array of GR_SC_COUNT doubles; see the GR_SC_* slots. */
+enum {
+  GR_SC_SOLD = 0,   /* <s_old, s_old> */
+  GR_SC_ALPHA = 1,  /* CG step, rounded to the data precision */
+  GR_SC_BETA = 2,   /* CG direction weight, rounded to the data precision */
+  GR_SC_DSQ = 3,    /* <d, d> */
+  GR_SC_FSQ = 4,    /* <sino, sino> */
+  GR_SC_RES = 5,    /* relative residual */
+  GR_SC_SUM = 6,    /* normest: current sum of the iterate */
+  GR_SC_COUNT = 8
+};
+/* CG scalar steps (gratopy.py:2523-2547):
+ * alpha = c * sold / sum(partials)           (c = delta_x^2 / delta_s)
+ * d -= alpha q  (+ block partials of <d, d>)
+ * sold <- sum(snew partials), beta = snew/sold, residual, done flag
+ * p = beta p + snew */
+GR_API int gr_cg_alpha(double* sc, const double* partials, size_t n, double c, int dtype,
+                const int* skip, void* stream);
+GR_API int gr_cg_update_d(void* d, const void* q, const double* sc, double* partials, int dtype,
+                   size_t n, const int* skip, void* stream);
+GR_API int gr_cg_beta(double* sc, const double* snew_partials, size_t n_snew,
+               const double* d_partials, size_t n_d, double epsilon, int dtype, int* done,
+               void* stream);
+GR_API int gr_cg_update_p(void* p, const void* snew, const double* sc, int dtype, size_t n,
+                   const int* skip, void* stream);
+/* normest: img /= (real) sc[GR_SC_SUM] */
+GR_API int gr_scale_by_sum(void* img, const double* sc, int dtype, size_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRATOPY_GB300_H */
