@@ -1,0 +1,336 @@
+"""Benchmark: fan-beam forward + backprojection throughput on one GB300.
+
+Workload (the fan-beam configuration the headline metric is quoted on):
+512 x 512 float32 image of 10 seeded random ellipses, fan beam, 360 angles
+over [0, 2 pi), 768 detectors, RE = 200, R = 400, detector width 400,
+image width 0.9 x the automatic width (the image fills 90% of the fan).
+A step is one forward projection plus one backprojection; the metric is
+pixel-angle pairs processed per second (Nx Ny Na for each projection).
+
+Timing: device time with CUDA events on the launching stream; the L2 cache
+(129 MB) is flushed by writing a 256 MB buffer before every timed step,
+outside the events.  ``e2e`` repeats the step through the public API with
+the image copied in from pinned host memory and the backprojection copied
+back, copies inside the timed region.
+
+``--impl reference`` times the CPU restatement of gratopy's kernels (the
+reference's OpenCL kernels need an OpenCL runtime that this machine lacks)
+on all host cores for the same workload and metric.
+
+Multi-GPU (``torchrun``): every rank runs the same single-GPU workload
+(independent replicas, no collective on the data path); the value is the
+sum over ranks divided by the slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "fwd+back Gpixel-angle/s"
+UNIT = "Gpixel-angle/s"
+
+WORKLOAD = dict(geometry="fanbeam", img_shape=(512, 512), angles=360, n_detectors=768,
+                detector_width=400.0, RE=200.0, R=400.0,
+                image_width=0.9 * (2 * 0.5 * 200.0 / np.sqrt(1 + 0.25)))
+SEED = 1234
+
+
+def peaks():
+    try:
+        d = json.loads(MEASURED_PEAKS.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def make_image(seed=SEED):
+    from gratopy_gb300.phantom import random_ellipse_image
+
+    img = random_ellipse_image(seed, (512, 512), count=10, dtype="float32")
+    return np.asfortranarray(img.T)  # (Nx, Ny), Fortran order
+
+
+def pixel_angles():
+    Nx, Ny = WORKLOAD["img_shape"]
+    return Nx * Ny * WORKLOAD["angles"]
+
+
+def config_block():
+    return {"workload": "fanbeam 512x512 float32, 360 angles [0,2pi), 768 detectors, RE=200, "
+                        "R=400, image width 0.9x automatic; step = forward + backprojection",
+            "image": [512, 512], "angles": 360, "detectors": 768, "RE": 200.0, "R": 400.0,
+            "l2": "flushed before every timed step (256 MB write)", "seed": SEED}
+
+
+# ------------------------------------------------------------------ clocks
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._proc = None
+        self._thread = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self._proc = None
+            return self
+
+        def reader():
+            for line in self._proc.stdout:
+                self.rows.append([c.strip() for c in line.split(",")])
+
+        self._thread = threading.Thread(target=reader, daemon=True)
+        self._thread.start()
+        return self
+
+    def stop(self):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+        if self._thread is not None:
+            self._thread.join(timeout=5)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- GPU arm
+
+
+def run_gpu(args, rank, world, device):
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import _lib
+
+    _lib.load()
+    cfg = dict(WORKLOAD)
+    cfg.pop("geometry")
+    img_shape = cfg.pop("img_shape")
+    angles = cfg.pop("angles")
+    ps = gg.ProjectionSettings(device, gg.FANBEAM, img_shape, angles, **cfg)
+    host = make_image()
+    img = gg.core.empty(img_shape, torch.float32, "F", device)
+    img.copy_(torch.from_numpy(np.ascontiguousarray(host.T)).T)
+    sino = gg.core.empty(ps.sinogram_shape, torch.float32, "F", device)
+    back = gg.core.empty(img_shape, torch.float32, "F", device)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        gg.forwardprojection(img, ps, sino=sino)
+        if ev is not None:
+            ev[1].record(stream)
+        gg.backprojection(sino, ps, img=back)
+        if ev is not None:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize(device)
+
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    sampler = ClockSampler(device.index).start() if rank == 0 else None
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(device)
+    for k in range(args.steps):
+        flush.zero_()
+        step(events[k])
+    torch.cuda.synchronize(device)
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop() if sampler is not None else None
+    t_fwd = [events[k][0].elapsed_time(events[k][1]) * 1e-3 for k in range(args.steps)]
+    t_bwd = [events[k][1].elapsed_time(events[k][2]) * 1e-3 for k in range(args.steps)]
+    total = sum(t_fwd) + sum(t_bwd)
+    if world > 1:
+        t = torch.tensor([total], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+
+    # end to end through the public API with host buffers
+    h_img = torch.from_numpy(np.ascontiguousarray(host.T)).pin_memory()
+    h_back = torch.empty((img_shape[1], img_shape[0]), dtype=torch.float32).pin_memory()
+    d_img = gg.core.empty(img_shape, torch.float32, "F", device)
+    e_events = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
+
+    def e2e_step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        d_img.T.copy_(h_img, non_blocking=True)
+        s = gg.forwardprojection(d_img, ps)
+        b = gg.backprojection(s, ps)
+        h_back.copy_(b.T, non_blocking=True)
+        if ev is not None:
+            ev[1].record(stream)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        e2e_step()
+    torch.cuda.synchronize(device)
+    for k in range(args.steps):
+        flush.zero_()
+        e2e_step(e_events[k])
+    torch.cuda.synchronize(device)
+    e2e_total = sum(e[0].elapsed_time(e[1]) * 1e-3 for e in e_events)
+    ok = np.allclose(h_back.numpy().T, back.cpu().numpy(), rtol=1e-6, atol=1e-6 * float(back.abs().max()))
+    if not ok:
+        raise RuntimeError("end-to-end result differs from the device-resident run")
+
+    return dict(total=total, t_fwd=t_fwd, t_bwd=t_bwd, clocks=clocks, e2e_total=e2e_total,
+                h2d=h_img.numel() * 4, d2h=h_back.numel() * 4, ps=ps)
+
+
+def cpu_baseline_sample(max_seconds=12.0):
+    """Time the oracle (restated reference kernels) on this host's cores."""
+    from oracle import oracle as O
+    from tests.helpers import host_settings
+
+    ps = host_settings(WORKLOAD)
+    img = make_image()
+    O.forward(img, ps)  # builds and loads the library outside the timing
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        sino = O.forward(img, ps)
+        O.backward(sino, ps)
+        reps += 1
+        if time.perf_counter() - t0 >= max_seconds or reps >= 50:
+            break
+    dt = time.perf_counter() - t0
+    value = 2 * pixel_angles() * reps / dt / 1e9
+    return {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
+            "sample": f"{reps} forward+back steps of the full workload, {dt:.1f} s wall"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gratopy_gb300", choices=["gratopy_gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = max(1, args.steps)
+        base = cpu_baseline_sample(max_seconds=min(60.0, 3.0 * steps))
+        line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "impl": "reference",
+                "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
+                "ms_per_step": 2 * pixel_angles() / base["value"] / 1e6,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic: seeded random ellipses",
+                "config": config_block(), "cpu_baseline": base,
+                "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    res = run_gpu(args, rank, world, device)
+
+    steps = args.steps
+    units = 2 * pixel_angles() * world
+    value = units * steps / res["total"] / 1e9
+    e2e = 2 * pixel_angles() * world * steps / res["e2e_total"] / 1e9
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    hbm, hbm_kind = peaks()
+    ps = res["ps"]
+    Ns, Na = ps.sinogram_shape
+    Nx, Ny = ps.img_shape
+    compulsory = (Nx * Ny + Ns * Na) * 4
+    fwd, bwd = statistics.mean(res["t_fwd"]), statistics.mean(res["t_bwd"])
+    dom, t_dom = ("fan_fwd_kernel", fwd) if fwd >= bwd else ("fan_bwd_kernel", bwd)
+    achieved = compulsory / t_dom / 1e9
+    traffic = None
+    tr_file = ROOT / "profiles" / "traffic.json"
+    if tr_file.exists():
+        try:
+            traffic = json.loads(tr_file.read_text()).get(dom)
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": res["total"] / steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded random ellipses (10 per image)",
+        "config": dict(config_block(), parallelism=f"replicas{world}"),
+        "fwd_gpixel_angle_per_s": pixel_angles() / fwd / 1e9,
+        "bwd_gpixel_angle_per_s": pixel_angles() / bwd / 1e9,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                     "algorithmic_bytes": compulsory, "peak_source": hbm_kind,
+                     "gather_bytes_per_s": 8 * pixel_angles() / t_dom / 1e9},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
+                "d2h_bytes_per_step": res["d2h"]},
+        "gpu_launches": 2 * steps,
+        "clocks": res["clocks"],
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample()
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -33,6 +33,8 @@ class GrGeometry(ctypes.Structure):
         ("ofs", ctypes.c_void_p),
         ("sdpd", ctypes.c_void_p),
         ("geo", ctypes.c_double * 11),
+        ("fwd_split", ctypes.c_int),
+        ("bwd_split", ctypes.c_int),
     ]
 
 

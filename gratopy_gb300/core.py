@@ -639,7 +639,7 @@ def normest(projectionsetting, number_iterations=50, dtype="float32", allocator=
         _lib.call("gr_sum_values_partials", _ptr(scr.dot), _ptr(img), _dt(img), n, st)
         _lib.call("gr_sum_partials", scr.slot(_lib.SC_SUM), _ptr(scr.dot), scr.dot.numel(), st)
         for i in range(number_iterations):
-            _lib.call("gr_scale_by_sum", _ptr(img), scr.slot(_lib.SC_SUM), _dt(img), n, st)
+            _lib.call("gr_scale_by_sum", _ptr(img), _ptr(scr.sc), _dt(img), n, st)
             _lib.call("gr_forward", ctypes.byref(g), _ptr(sino), _ptr(img), 1, 0, 0, st)
             _lib.call("gr_backward_sum", ctypes.byref(g), _ptr(img), _ptr(sino), _ptr(scr.part), 1,
                       0, st)

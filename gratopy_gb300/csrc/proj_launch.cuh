@@ -1,0 +1,231 @@
+// Launch helpers shared by the projection translation units: geometry
+// checks, launch-shape selection (z-block, lanes per bin, angle groups) and
+// the templated kernel launches.
+#pragma once
+
+#include "gr_internal.cuh"
+#include "projection.cuh"
+
+namespace gr {
+namespace launch {
+
+
+inline int check_geometry(const gr_geometry* g) {
+  if (g == nullptr || g->ofs == nullptr) return GR_ERR_ARG;
+  if (g->kind != GR_RADON && g->kind != GR_FANBEAM) return GR_ERR_ARG;
+  if (!valid_dtype(g->dtype)) return GR_ERR_ARG;
+  if (g->kind == GR_FANBEAM && g->sdpd == nullptr) return GR_ERR_ARG;
+  if (g->Nx <= 0 || g->Ny <= 0 || g->Ns <= 0 || g->Na <= 0) return GR_ERR_SHAPE;
+  if (g->Na > 65535) return GR_ERR_TOO_BIG;
+  return GR_OK;
+}
+
+inline Dims dims_of(const gr_geometry* g, int Nz) {
+  Dims d;
+  d.Nx = g->Nx;
+  d.Ny = g->Ny;
+  d.Nz = Nz;
+  d.Ns = g->Ns;
+  d.Na = g->Na;
+  return d;
+}
+
+template <typename T>
+inline RadonGeo<T> radon_geo(const double* geo) {
+  RadonGeo<T> r;
+  r.delta_x = (float)geo[0];
+  r.delta_xi = (float)geo[1];
+  return r;
+}
+
+template <typename T>
+inline FanGeo<T> fan_geo(const double* geo) {
+  FanGeo<T> f;
+  f.R = (T)geo[0];
+  f.RE = (T)geo[1];
+  f.delta_xi = (T)geo[2];
+  f.midx = (T)geo[3];
+  f.midy = (T)geo[4];
+  f.mid_det = (T)geo[5];
+  f.delta_x = (T)geo[10];
+  return f;
+}
+
+inline int zblock(int Nz) { return Nz == 1 ? 1 : 4; }
+
+// Resident threads the device holds (SM count x 2048), cached per device.
+inline int64_t device_capacity() {
+  static int64_t cap[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152 * 2048;
+  if (cap[dev] == 0) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      sms = 152;
+    cap[dev] = (int64_t)sms * 2048;
+  }
+  return cap[dev];
+}
+
+inline bool valid_split(int v) { return v == 1 || v == 2 || v == 4 || v == 8; }
+
+// Lanes per detector bin: enough that the launch holds about two waves of
+// resident threads (small problems), 1 for large ones.
+// float64 launches use 1 or 4 only (fewer instantiations; float64 is the
+// parity path, not the throughput path).
+inline int clamp_split(const gr_geometry* g, int sp) {
+  return g->dtype == GR_F64 ? (sp >= 4 ? 4 : 1) : sp;
+}
+
+inline int fwd_split(const gr_geometry* g, int Nz) {
+  if (valid_split(g->fwd_split)) return clamp_split(g, g->fwd_split);
+  const int64_t work = (int64_t)g->Ns * g->Na * ((Nz + zblock(Nz) - 1) / zblock(Nz));
+  const int64_t want = 2 * device_capacity();
+  for (int sp = 1; sp < 8; sp <<= 1)
+    if (work * sp >= want) return clamp_split(g, sp);
+  return clamp_split(g, 8);
+}
+
+inline int bwd_split(const gr_geometry* g, int Nz) {
+  if (valid_split(g->bwd_split)) return clamp_split(g, g->bwd_split);
+  const int64_t work = (int64_t)g->Nx * g->Ny * ((Nz + zblock(Nz) - 1) / zblock(Nz));
+  const int64_t want = 2 * device_capacity();
+  for (int sp = 1; sp < 8; sp <<= 1)
+    if (work * sp >= want) return clamp_split(g, sp);
+  return clamp_split(g, 8);
+}
+
+inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
+  const int ZB = zblock(Nz);
+  const int per_block = (32 / split) * (kFwdBlock / 32);
+  return dim3((g->Ns + per_block - 1) / per_block, g->Na, (Nz + ZB - 1) / ZB);
+}
+
+inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
+  const int ZB = zblock(Nz);
+  const int fast = io == ORDER_F ? g->Nx : g->Ny;
+  const int slow = io == ORDER_F ? g->Ny : g->Nx;
+  const int rows = kBwdTileSlow / split;
+  return dim3((fast + kBwdTileFast - 1) / kBwdTileFast, (slow + rows - 1) / rows, (Nz + ZB - 1) / ZB);
+}
+
+template <typename T, int SO, int IO, int ZB, int SPLIT, class Epi>
+int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* partials,
+                  const int* skip, cudaStream_t st) {
+  const Dims d = dims_of(g, Nz);
+  const dim3 grid = fwd_grid(g, Nz, SPLIT);
+  if (g->kind == GR_RADON) {
+    radon_fwd_kernel<T, SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+        img, static_cast<const T*>(g->ofs), radon_geo<T>(g->geo), d, epi, partials, skip);
+  } else {
+    fan_fwd_kernel<T, SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+        img, static_cast<const T*>(g->ofs), static_cast<const T*>(g->sdpd), fan_geo<T>(g->geo), d,
+        epi, partials, skip);
+  }
+  return check_launch();
+}
+
+template <typename T, int SO, int IO, int ZB, class Epi>
+int launch_fwd_split(const gr_geometry* g, const T* img, int Nz, Epi epi, double* partials,
+                     const int* skip, cudaStream_t st) {
+  const int sp = fwd_split(g, Nz);
+  if constexpr (std::is_same<T, double>::value) {
+    if (sp == 1) return launch_fwd_zb<T, SO, IO, ZB, 1>(g, img, Nz, epi, partials, skip, st);
+    return launch_fwd_zb<T, SO, IO, ZB, 4>(g, img, Nz, epi, partials, skip, st);
+  } else {
+    switch (sp) {
+      case 1: return launch_fwd_zb<T, SO, IO, ZB, 1>(g, img, Nz, epi, partials, skip, st);
+      case 2: return launch_fwd_zb<T, SO, IO, ZB, 2>(g, img, Nz, epi, partials, skip, st);
+      case 4: return launch_fwd_zb<T, SO, IO, ZB, 4>(g, img, Nz, epi, partials, skip, st);
+      default: return launch_fwd_zb<T, SO, IO, ZB, 8>(g, img, Nz, epi, partials, skip, st);
+    }
+  }
+}
+
+template <typename T, int SO, int IO, class Epi>
+int launch_fwd(const gr_geometry* g, const void* img, int Nz, Epi epi, double* partials,
+               const int* skip, void* stream) {
+  int rc = check_geometry(g);
+  if (rc) return rc;
+  if (img == nullptr || Nz <= 0) return GR_ERR_ARG;
+  if ((Nz + 3) / 4 > 65535) return GR_ERR_TOO_BIG;
+  const T* im = static_cast<const T*>(img);
+  if (Nz == 1) return launch_fwd_split<T, SO, IO, 1>(g, im, Nz, epi, partials, skip, as_stream(stream));
+  return launch_fwd_split<T, SO, IO, 4>(g, im, Nz, epi, partials, skip, as_stream(stream));
+}
+
+template <typename T, int IO, int SO, int ZB, int SPLIT, class Epi>
+int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* partials,
+                  const int* skip, cudaStream_t st) {
+  const Dims d = dims_of(g, Nz);
+  const dim3 grid = bwd_grid(g, Nz, IO, SPLIT);
+  const dim3 block(kBwdTileFast, kBwdTileSlow);
+  if (g->kind == GR_RADON) {
+    radon_bwd_kernel<T, IO, SO, ZB, SPLIT, Epi><<<grid, block, 0, st>>>(
+        sino, static_cast<const T*>(g->ofs), d, epi, partials, skip);
+  } else {
+    fan_bwd_kernel<T, IO, SO, ZB, SPLIT, Epi><<<grid, block, 0, st>>>(
+        sino, static_cast<const T*>(g->ofs), static_cast<const T*>(g->sdpd), fan_geo<T>(g->geo), d,
+        epi, partials, skip);
+  }
+  return check_launch();
+}
+
+template <typename T, int IO, int SO, int ZB, class Epi>
+int launch_bwd_split(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* partials,
+                     const int* skip, cudaStream_t st) {
+  const int sp = bwd_split(g, Nz);
+  if constexpr (std::is_same<T, double>::value) {
+    if (sp == 1) return launch_bwd_zb<T, IO, SO, ZB, 1>(g, sino, Nz, epi, partials, skip, st);
+    return launch_bwd_zb<T, IO, SO, ZB, 4>(g, sino, Nz, epi, partials, skip, st);
+  } else {
+    switch (sp) {
+      case 1: return launch_bwd_zb<T, IO, SO, ZB, 1>(g, sino, Nz, epi, partials, skip, st);
+      case 2: return launch_bwd_zb<T, IO, SO, ZB, 2>(g, sino, Nz, epi, partials, skip, st);
+      case 4: return launch_bwd_zb<T, IO, SO, ZB, 4>(g, sino, Nz, epi, partials, skip, st);
+      default: return launch_bwd_zb<T, IO, SO, ZB, 8>(g, sino, Nz, epi, partials, skip, st);
+    }
+  }
+}
+
+template <typename T, int IO, int SO, class Epi>
+int launch_bwd(const gr_geometry* g, const void* sino, int Nz, Epi epi, double* partials,
+               const int* skip, void* stream) {
+  int rc = check_geometry(g);
+  if (rc) return rc;
+  if (sino == nullptr || Nz <= 0) return GR_ERR_ARG;
+  if ((Nz + 3) / 4 > 65535) return GR_ERR_TOO_BIG;
+  const T* sn = static_cast<const T*>(sino);
+  if (Nz == 1) return launch_bwd_split<T, IO, SO, 1>(g, sn, Nz, epi, partials, skip, as_stream(stream));
+  return launch_bwd_split<T, IO, SO, 4>(g, sn, Nz, epi, partials, skip, as_stream(stream));
+}
+
+// Fills a gr_geometry from the reference-style argument list.
+inline gr_geometry make_geo(int kind, int dtype, const void* ofs, const void* sdpd, const double* geo) {
+  gr_geometry g;
+  g.kind = kind;
+  g.dtype = dtype;
+  g.fwd_split = 0;
+  g.bwd_split = 0;
+  g.ofs = ofs;
+  g.sdpd = sdpd;
+  const int n = kind == GR_RADON ? 6 : 11;
+  for (int i = 0; i < 11; ++i) g.geo[i] = i < n && geo ? geo[i] : 0.0;
+  if (geo == nullptr) {
+    g.Nx = g.Ny = g.Ns = g.Na = 0;
+  } else if (kind == GR_RADON) {
+    g.Nx = (int)geo[2];
+    g.Ny = (int)geo[3];
+    g.Ns = (int)geo[4];
+    g.Na = (int)geo[5];
+  } else {
+    g.Nx = (int)geo[6];
+    g.Ny = (int)geo[7];
+    g.Ns = (int)geo[8];
+    g.Na = (int)geo[9];
+  }
+  return g;
+}
+
+}  // namespace launch
+}  // namespace gr

@@ -11,6 +11,8 @@
 // (radon_ad), fanbeam.cl:72-256 (fanbeam), fanbeam.cl:290-391 (fanbeam_ad).
 #pragma once
 
+#include <type_traits>
+
 #include "gr_common.cuh"
 
 namespace gr {
@@ -170,20 +172,63 @@ struct BwdTVPrimal {
   }
 };
 
+// ------------------------------------------------------------------ helpers
+
+// Per-angle record of the Radon backprojection staged in shared memory.
+template <typename T>
+struct alignas(sizeof(T) * 4) RadonAngle {
+  T X, Y, off, w;
+};
+
+// Warp layout of the forward kernels: a warp holds 32/SPLIT consecutive
+// detector bins of one angle; the SPLIT lanes of a bin walk interleaved image
+// rows and are summed with warp shuffles (fixed xor order: deterministic).
+template <int SPLIT>
+struct FwdLayout {
+  static constexpr int kRaysPerWarp = 32 / SPLIT;
+  static constexpr int kRaysPerBlock = kRaysPerWarp * (kFwdBlock / 32);
+  int64_t s;
+  int group;
+  __device__ __forceinline__ FwdLayout() {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    s = (int64_t)blockIdx.x * kRaysPerBlock + warp * kRaysPerWarp + (lane % kRaysPerWarp);
+    group = lane / kRaysPerWarp;
+  }
+};
+
+template <int SPLIT, typename T, int ZB>
+__device__ __forceinline__ void warp_reduce_rows(T (&acc)[ZB]) {
+#pragma unroll
+  for (int o = 32 / SPLIT; o < 32; o <<= 1) {
+#pragma unroll
+    for (int k = 0; k < ZB; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+  }
+}
+
+// Reciprocal used by the float32 fan kernels: one hardware approximation
+// (relative error ~1e-7, far inside the float32 tolerance); float64 keeps
+// the reference's exact divisions.
+__device__ __forceinline__ float fast_rcp(float v) { return __fdividef(1.0f, v); }
+
 // ------------------------------------------------------------- Radon forward
-// radon.cl:66-161.  One thread per (detector bin s, angle a) and ZB slices.
+// radon.cl:66-161.  One detector bin per SPLIT lanes, ZB slices per thread.
 // ofs: 8 reals per angle (X, Y, offset, 1/max, weight, flip, -, -).
-template <typename T, int SO, int IO, int ZB, class Epi>
+template <typename T, int SO, int IO, int ZB, int SPLIT, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
 radon_fwd_kernel(const T* __restrict__ img, const T* __restrict__ ofs, RadonGeo<T> g, Dims d,
                  Epi epi, double* __restrict__ partials, const int* __restrict__ skip) {
   __shared__ double red[kFwdBlock / 32];
   if (skip != nullptr && *skip) return;
-  const int64_t s = (int64_t)blockIdx.x * kFwdBlock + threadIdx.x;
+  const FwdLayout<SPLIT> L;
+  const int64_t s = L.s;
   const int64_t a = blockIdx.y;
   const int64_t z0 = (int64_t)blockIdx.z * ZB;
-  double part = 0.0;
-  if (s < d.Ns) {
+  const bool active = s < d.Ns;
+  const int zn = (int)min((int64_t)ZB, d.Nz - z0);
+  T acc[ZB];
+#pragma unroll
+  for (int k = 0; k < ZB; ++k) acc[k] = (T)0.;
+  if (active) {
     const T* o8 = ofs + 8 * a;
     T ox = o8[0], oy = o8[1];
     const T oz = o8[2], ow = o8[3];
@@ -200,12 +245,8 @@ radon_fwd_kernel(const T* __restrict__ img, const T* __restrict__ ofs, RadonGeo<
       step_y = sx;
     }
     const T* img0 = img + z0 * sz;
-    int zn = (int)min((int64_t)ZB, d.Nz - z0);
-    T acc[ZB];
-#pragma unroll
-    for (int k = 0; k < ZB; ++k) acc[k] = (T)0.;
     const T fs = (T)(int)s;
-    for (int y = 0; y < Nyy; ++y) {
+    for (int y = L.group; y < Nyy; y += SPLIT) {
       const T dd = (T)y * oy + oz - fs;
       int x_low = (int)((-1 - dd) * ow);
       int x_high = (int)((1 - dd) * ow);
@@ -215,14 +256,20 @@ radon_fwd_kernel(const T* __restrict__ img, const T* __restrict__ ofs, RadonGeo<
       const T* p = img0 + (int64_t)y * step_y + (int64_t)x_low * step_x;
       for (int x = x_low; x <= x_high; ++x) {
         const T w = (T)1. - gabs((T)x * ox + dd);
+        T v[ZB];
+#pragma unroll
+        for (int k = 0; k < ZB; ++k) v[k] = k < zn ? ldg(p + k * sz) : (T)0.;
         if (w > (T)0.) {
 #pragma unroll
-          for (int k = 0; k < ZB; ++k)
-            if (k < zn) acc[k] += w * ldg(p + k * sz);
+          for (int k = 0; k < ZB; ++k) acc[k] += w * v[k];
         }
         p += step_x;
       }
     }
+  }
+  if (SPLIT > 1) warp_reduce_rows<SPLIT>(acc);
+  double part = 0.0;
+  if (active && L.group == 0) {
 #pragma unroll
     for (int k = 0; k < ZB; ++k) {
       if (k < zn) {
@@ -239,103 +286,27 @@ radon_fwd_kernel(const T* __restrict__ img, const T* __restrict__ ofs, RadonGeo<
   }
 }
 
-// ------------------------------------------------------------ Radon backward
-// radon.cl:183-241.  Block = 32 x 8 pixels along (fast, slow) axis; the fast
-// axis is x for F-ordered images and y for C-ordered ones.
-template <typename T>
-struct alignas(sizeof(T) * 4) RadonAngle {
-  T X, Y, off, w;
-};
-
-template <int IO>
-__device__ __forceinline__ void bwd_pixel(int64_t& x, int64_t& y) {
-  const int64_t f = (int64_t)blockIdx.x * kBwdTileFast + threadIdx.x;
-  const int64_t sl = (int64_t)blockIdx.y * kBwdTileSlow + threadIdx.y;
-  if (IO == ORDER_F) { x = f; y = sl; } else { y = f; x = sl; }
-}
-
-template <typename T, int IO, int SO, int ZB, class Epi>
-__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
-radon_bwd_kernel(const T* __restrict__ sino, const T* __restrict__ ofs, Dims d, Epi epi,
-                 double* __restrict__ partials, const int* __restrict__ skip) {
-  __shared__ RadonAngle<T> sang[kAngleChunk];
-  __shared__ double red[kBwdTileFast * kBwdTileSlow / 32];
-  if (skip != nullptr && *skip) return;
-  int64_t x, y;
-  bwd_pixel<IO>(x, y);
-  const int64_t z0 = (int64_t)blockIdx.z * ZB;
-  const bool active = x < d.Nx && y < d.Ny;
-  const int zn = (int)min((int64_t)ZB, d.Nz - z0);
-  int64_t ss_, sa_, sz_;
-  sino_strides<SO>(d, ss_, sa_, sz_);
-  const T* sn = sino + z0 * sz_;
-  const int Ns = (int)d.Ns;
-  const T cx = (T)x, cy = (T)y;
-  T acc[ZB];
-#pragma unroll
-  for (int k = 0; k < ZB; ++k) acc[k] = (T)0.;
-  const int tid = threadIdx.x + kBwdTileFast * threadIdx.y;
-  for (int a0 = 0; a0 < d.Na; a0 += kAngleChunk) {
-    const int na = (int)min((int64_t)kAngleChunk, d.Na - a0);
-    __syncthreads();
-    for (int j = tid; j < na; j += kBwdTileFast * kBwdTileSlow) {
-      const T* o = ofs + 8 * (int64_t)(a0 + j);
-      RadonAngle<T> r;
-      r.X = o[0];
-      r.Y = o[1];
-      r.off = o[2];
-      r.w = o[4];
-      sang[j] = r;
-    }
-    __syncthreads();
-    if (active) {
-      for (int j = 0; j < na; ++j) {
-        const RadonAngle<T> r = sang[j];
-        const T s = cx * r.X + cy * r.Y + r.off;
-        int sm = (int)gfloor(s);
-        int sp = sm + 1;
-        T wp = (T)1 - ((T)sp - s);
-        T wm = (T)1 - (s - (T)sm);
-        if (sm < 0 || sm >= Ns) { wm = (T)0.; sm = 0; }
-        if (sp < 0 || sp >= Ns) { wp = (T)0.; sp = 0; }
-        const int64_t base = (int64_t)(a0 + j) * sa_;
-        const T* pm = sn + base + (int64_t)sm * ss_;
-        const T* pp = sn + base + (int64_t)sp * ss_;
-#pragma unroll
-        for (int k = 0; k < ZB; ++k)
-          if (k < zn) acc[k] += r.w * (wm * ldg(pm + k * sz_) + wp * ldg(pp + k * sz_));
-      }
-    }
-  }
-  double part = 0.0;
-  if (active) {
-#pragma unroll
-    for (int k = 0; k < ZB; ++k)
-      if (k < zn) part += epi(x, y, z0 + k, img_index<IO>(x, y, z0 + k, d), acc[k]);
-  }
-  if (Epi::kReduce) {
-    double t = block_sum(part, red);
-    if (tid == 0)
-      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
-  }
-}
-
 // --------------------------------------------------------------- Fan forward
-// fanbeam.cl:72-256.  One thread per (detector bin, angle) and ZB slices.
-template <typename T, int SO, int IO, int ZB, class Epi>
+// fanbeam.cl:72-256.  Same layout as the Radon forward kernel.
+template <typename T, int SO, int IO, int ZB, int SPLIT, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
 fan_fwd_kernel(const T* __restrict__ img, const T* __restrict__ ofs, const T* __restrict__ sdpd,
                FanGeo<T> g, Dims d, Epi epi, double* __restrict__ partials,
                const int* __restrict__ skip) {
   __shared__ double red[kFwdBlock / 32];
   if (skip != nullptr && *skip) return;
-  const int64_t s = (int64_t)blockIdx.x * kFwdBlock + threadIdx.x;
+  const FwdLayout<SPLIT> L;
+  const int64_t s = L.s;
   const int64_t a = blockIdx.y;
   const int64_t z0 = (int64_t)blockIdx.z * ZB;
-  double part = 0.0;
-  if (s < d.Ns) {
+  const bool active = s < d.Ns;
+  const int zn = (int)min((int64_t)ZB, d.Nz - z0);
+  T acc[ZB];
+#pragma unroll
+  for (int k = 0; k < ZB; ++k) acc[k] = (T)0.;
+  const T R = g.R, dxi = g.delta_xi;
+  if (active) {
     T midx = g.midx, midy = g.midy;
-    const T R = g.R, dxi = g.delta_xi;
     T RE = g.RE;
     const T* o = ofs + 8 * a;
     T dx = o[0], dy = o[1], qx = o[2], qy = o[3];
@@ -379,11 +350,7 @@ fan_fwd_kernel(const T* __restrict__ img, const T* __restrict__ ofs, const T* __
     const T hi_lim = (T)(Nxx - 1) - midx;
     const T lo_lim = -midx;
     const T* img0 = img + z0 * sz;
-    const int zn = (int)min((int64_t)ZB, d.Nz - z0);
-    T acc[ZB];
-#pragma unroll
-    for (int k = 0; k < ZB; ++k) acc[k] = (T)0.;
-    for (int y = 0; y < Nyy; ++y) {
+    for (int y = L.group; y < Nyy; y += SPLIT) {
       const T yr = (T)y;
       const T xhigh = qx + dpx * (yr - midy - qy);
       const T xlow = qx + dmx * (yr - midy - qy);
@@ -394,8 +361,14 @@ fan_fwd_kernel(const T* __restrict__ img, const T* __restrict__ ofs, const T* __
       T ss = dx * ((T)xlo - midx) + dy * (yr - midy);
       const T* p = img0 + (int64_t)y * step_y + (int64_t)xlo * step_x;
       for (int x = xlo; x <= xhi; ++x) {
-        const T xi = ss / t;
-        const T W = ((T)1. - gabs(s_mid - xi)) / t;
+        T W;
+        if constexpr (std::is_same<T, float>::value) {
+          const float r = fast_rcp(t);
+          W = (1.0f - fabsf(s_mid - ss * r)) * r;
+        } else {
+          const T xi = ss / t;
+          W = ((T)1. - gabs(s_mid - xi)) / t;
+        }
 #pragma unroll
         for (int k = 0; k < ZB; ++k)
           if (k < zn) acc[k] += W * ldg(p + k * sz);
@@ -404,6 +377,10 @@ fan_fwd_kernel(const T* __restrict__ img, const T* __restrict__ ofs, const T* __
         ss += dx;
       }
     }
+  }
+  if (SPLIT > 1) warp_reduce_rows<SPLIT>(acc);
+  double part = 0.0;
+  if (active && L.group == 0) {
     const T sd = sdpd[s];
 #pragma unroll
     for (int k = 0; k < ZB; ++k) {
@@ -421,25 +398,148 @@ fan_fwd_kernel(const T* __restrict__ img, const T* __restrict__ ofs, const T* __
   }
 }
 
-// -------------------------------------------------------------- Fan backward
-// fanbeam.cl:290-391.  Per angle: detector direction scaled by 1/dxi^2,
-// source-to-detector-foot direction scaled by 1/R^2, source position and
-// angle weight, precomputed once per block into shared memory.
-template <typename T>
-struct alignas(sizeof(T) * 8) FanAngle {
-  T ddx, ddy, dx, dy, qx, qy, w, pad;
+// ------------------------------------------------------------ backprojection
+// Block = 32 lanes along the contiguous pixel axis (x for F images, y for C
+// images) x 8 thread rows.  With angle split ASPLIT, ASPLIT consecutive
+// thread rows share one pixel row and take interleaved angles; their partial
+// sums are added in a fixed order through shared memory (deterministic).
+template <int ASPLIT>
+struct BwdLayout {
+  static constexpr int kRows = kBwdTileSlow / ASPLIT;
+  int64_t fast, slow;
+  int g;
+  __device__ __forceinline__ BwdLayout() {
+    g = threadIdx.y % ASPLIT;
+    fast = (int64_t)blockIdx.x * kBwdTileFast + threadIdx.x;
+    slow = (int64_t)blockIdx.y * kRows + threadIdx.y / ASPLIT;
+  }
 };
 
-template <typename T, int IO, int SO, int ZB, class Epi>
+template <typename T, int ZB, int ASPLIT>
+struct BwdReduce {
+  T v[kBwdTileSlow][ZB][kBwdTileFast];
+};
+template <typename T, int ZB>
+struct BwdReduce<T, ZB, 1> {};
+
+template <typename T, int ZB, int ASPLIT>
+__device__ __forceinline__ void bwd_combine(T (&acc)[ZB], BwdReduce<T, ZB, ASPLIT>& red, int g) {
+  if constexpr (ASPLIT == 1) {
+    return;
+  } else {
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < ZB; ++k) red.v[threadIdx.y][k][threadIdx.x] = acc[k];
+  __syncthreads();
+  if (g == 0) {
+#pragma unroll
+    for (int k = 0; k < ZB; ++k) {
+      T t = red.v[threadIdx.y][k][threadIdx.x];
+#pragma unroll
+      for (int j = 1; j < ASPLIT; ++j) t += red.v[threadIdx.y + j][k][threadIdx.x];
+      acc[k] = t;
+    }
+  }
+  }
+}
+
+// radon.cl:183-241.
+template <typename T, int IO, int SO, int ZB, int ASPLIT, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+radon_bwd_kernel(const T* __restrict__ sino, const T* __restrict__ ofs, Dims d, Epi epi,
+                 double* __restrict__ partials, const int* __restrict__ skip) {
+  __shared__ RadonAngle<T> sang[kAngleChunk];
+  __shared__ double red[kBwdTileFast * kBwdTileSlow / 32];
+  __shared__ BwdReduce<T, ZB, ASPLIT> cred;
+  if (skip != nullptr && *skip) return;
+  const BwdLayout<ASPLIT> L;
+  const int64_t x = IO == ORDER_F ? L.fast : L.slow;
+  const int64_t y = IO == ORDER_F ? L.slow : L.fast;
+  const int64_t z0 = (int64_t)blockIdx.z * ZB;
+  const bool active = x < d.Nx && y < d.Ny;
+  const int zn = (int)min((int64_t)ZB, d.Nz - z0);
+  int64_t ss_, sa_, sz_;
+  sino_strides<SO>(d, ss_, sa_, sz_);
+  const T* sn = sino + z0 * sz_;
+  const int Ns = (int)d.Ns;
+  const T cx = (T)x, cy = (T)y;
+  T acc[ZB];
+#pragma unroll
+  for (int k = 0; k < ZB; ++k) acc[k] = (T)0.;
+  const int tid = threadIdx.x + kBwdTileFast * threadIdx.y;
+  for (int a0 = 0; a0 < d.Na; a0 += kAngleChunk) {
+    const int na = (int)min((int64_t)kAngleChunk, d.Na - a0);
+    __syncthreads();
+    for (int j = tid; j < na; j += kBwdTileFast * kBwdTileSlow) {
+      const T* o = ofs + 8 * (int64_t)(a0 + j);
+      RadonAngle<T> r;
+      r.X = o[0];
+      r.Y = o[1];
+      r.off = o[2];
+      r.w = o[4];
+      sang[j] = r;
+    }
+    __syncthreads();
+    if (active) {
+      for (int j = L.g; j < na; j += ASPLIT) {
+        const RadonAngle<T> r = sang[j];
+        const T s = cx * r.X + cy * r.Y + r.off;
+        const T fl = gfloor(s);
+        int sm = (int)fl;
+        int sp = sm + 1;
+        T wp, wm;
+        if constexpr (std::is_same<T, float>::value) {
+          wp = s - fl;
+          wm = 1.0f - wp;
+        } else {
+          wp = (T)1 - ((T)sp - s);
+          wm = (T)1 - (s - (T)sm);
+        }
+        if (sm < 0 || sm >= Ns) { wm = (T)0.; sm = 0; }
+        if (sp < 0 || sp >= Ns) { wp = (T)0.; sp = 0; }
+        const int64_t base = (int64_t)(a0 + j) * sa_;
+        const T* pm = sn + base + (int64_t)sm * ss_;
+        const T* pp = sn + base + (int64_t)sp * ss_;
+#pragma unroll
+        for (int k = 0; k < ZB; ++k)
+          if (k < zn) acc[k] += r.w * (wm * ldg(pm + k * sz_) + wp * ldg(pp + k * sz_));
+      }
+    }
+  }
+  bwd_combine<T, ZB, ASPLIT>(acc, cred, L.g);
+  double part = 0.0;
+  if (active && L.g == 0) {
+#pragma unroll
+    for (int k = 0; k < ZB; ++k)
+      if (k < zn) part += epi(x, y, z0 + k, img_index<IO>(x, y, z0 + k, d), acc[k]);
+  }
+  if (Epi::kReduce) {
+    double t = block_sum(part, red);
+    if (tid == 0)
+      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
+  }
+}
+
+// fanbeam.cl:290-391.  Per angle: detector direction scaled by 1/dxi^2,
+// source-to-detector-foot direction scaled by 1/R^2, source position and
+// angle weight (divided by R in the float32 path), staged in shared memory.
+template <typename T>
+struct alignas(sizeof(T) * 8) FanAngle {
+  T ddx, ddy, dx, dy, qx, qy, w, wR;
+};
+
+template <typename T, int IO, int SO, int ZB, int ASPLIT, class Epi>
 __global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
 fan_bwd_kernel(const T* __restrict__ sino, const T* __restrict__ ofs, const T* __restrict__ sdpd,
                FanGeo<T> g, Dims d, Epi epi, double* __restrict__ partials,
                const int* __restrict__ skip) {
   __shared__ FanAngle<T> sang[kAngleChunk];
   __shared__ double red[kBwdTileFast * kBwdTileSlow / 32];
+  __shared__ BwdReduce<T, ZB, ASPLIT> cred;
   if (skip != nullptr && *skip) return;
-  int64_t x, y;
-  bwd_pixel<IO>(x, y);
+  const BwdLayout<ASPLIT> L;
+  const int64_t x = IO == ORDER_F ? L.fast : L.slow;
+  const int64_t y = IO == ORDER_F ? L.slow : L.fast;
   const int64_t z0 = (int64_t)blockIdx.z * ZB;
   const bool active = x < d.Nx && y < d.Ny;
   const int zn = (int)min((int64_t)ZB, d.Nz - z0);
@@ -468,35 +568,57 @@ fan_bwd_kernel(const T* __restrict__ sino, const T* __restrict__ ofs, const T* _
       r.dx = o[0] * dxi_sqr_inv;
       r.dy = o[1] * dxi_sqr_inv;
       r.w = o[6];
-      r.pad = (T)0.;
+      r.wR = o[6] / R;
       sang[j] = r;
     }
     __syncthreads();
     if (active) {
-      for (int j = 0; j < na; ++j) {
+      for (int j = L.g; j < na; j += ASPLIT) {
         const FanAngle<T> r = sang[j];
         const T pqx = Px - r.qx, pqy = Py - r.qy;
         const T t = r.ddx * pqx + r.ddy * pqy;
         const T ss = r.dx * pqx + r.dy * pqy;
-        const T xi = ss / t + g.mid_det;
-        int xim = (int)gfloor(xi);
+        T xi, scale;
+        if constexpr (std::is_same<T, float>::value) {
+          const float inv = fast_rcp(t);
+          xi = ss * inv + g.mid_det;
+          scale = r.wR * inv;
+        } else {
+          xi = ss / t + g.mid_det;
+          scale = (T)0.;
+        }
+        const T fl = gfloor(xi);
+        int xim = (int)fl;
         int xip = xim + 1;
-        T Wp = (T)1. - ((T)xip - xi);
-        T Wm = (T)1. - (xi - (T)xim);
+        T Wp, Wm;
+        if constexpr (std::is_same<T, float>::value) {
+          Wp = xi - fl;
+          Wm = 1.0f - Wp;
+        } else {
+          Wp = (T)1. - ((T)xip - xi);
+          Wm = (T)1. - (xi - (T)xim);
+        }
         if (xim < 0 || xim >= Ns) { Wm = (T)0.; xim = 0; } else { Wm *= ldg(sdpd + xim); }
         if (xip < 0 || xip >= Ns) { Wp = (T)0.; xip = 0; } else { Wp *= ldg(sdpd + xip); }
-        const T scale = (R * t);
         const int64_t base = (int64_t)(a0 + j) * sa_;
         const T* pm = sn + base + (int64_t)xim * ss_;
         const T* pp = sn + base + (int64_t)xip * ss_;
+        if constexpr (std::is_same<T, float>::value) {
 #pragma unroll
-        for (int k = 0; k < ZB; ++k)
-          if (k < zn) acc[k] += r.w * (Wm * ldg(pm + k * sz_) + Wp * ldg(pp + k * sz_)) / scale;
+          for (int k = 0; k < ZB; ++k)
+            if (k < zn) acc[k] += scale * (Wm * ldg(pm + k * sz_) + Wp * ldg(pp + k * sz_));
+        } else {
+          const T rt = R * t;
+#pragma unroll
+          for (int k = 0; k < ZB; ++k)
+            if (k < zn) acc[k] += r.w * (Wm * ldg(pm + k * sz_) + Wp * ldg(pp + k * sz_)) / rt;
+        }
       }
     }
   }
+  bwd_combine<T, ZB, ASPLIT>(acc, cred, L.g);
   double part = 0.0;
-  if (active) {
+  if (active && L.g == 0) {
 #pragma unroll
     for (int k = 0; k < ZB; ++k)
       if (k < zn) part += epi(x, y, z0 + k, img_index<IO>(x, y, z0 + k, d), acc[k]);

