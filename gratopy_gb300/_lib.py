@@ -63,6 +63,7 @@ SIGNATURES = {
     "gr_forward_wsq": (_I, [_G, _P, _P, _P, _P, _P, _I, _I, _P]),
     "gr_backward_cg": (_I, [_G, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "gr_backward_sum": (_I, [_G, _P, _P, _P, _I, _I, _P]),
+    "gr_forward_wsq_noalloc": (_I, [_G, _P, _P, _P, _P, _I, _I, _P]),
     "gr_forward_partials": (_Z, [_G, _I]),
     "gr_backward_partials": (_Z, [_G, _I, _I]),
     "gr_weight_sinogram": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),

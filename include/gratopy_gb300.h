@@ -117,6 +117,19 @@ GR_API int gr_forward_wsq(const gr_geometry* g, void* q, const void* p, const vo
 GR_API int gr_backward_cg(const gr_geometry* g, void* snew, const void* d, void* x, const void* p,
                    const double* alpha, double* partials, const int* skip, int Nz, int order,
                    void* stream);
+/* No counterpart in the reference: gr_forward_wsq without caller scratch, for
+ * callers that cannot allocate device memory where they run this step (code
+ * inside a CUDA graph capture, hosts whose device memory is budgeted by
+ * another allocator, loops that cannot take cudaMalloc's implicit sync).
+ * Writes q = A p and *out = <W q, q> (device double).  The block partials
+ * live in a static device array of this library: at most 65536 of them
+ * (gr_forward_partials(g, Nz) <= 65536, else GR_ERR_TOO_BIG); 512 KiB is
+ * held on every GPU that loads the library until exit.  The first call on
+ * each device looks that array's address up (cudaGetSymbolAddress), so make
+ * it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race. */
+GR_API int gr_forward_wsq_noalloc(const gr_geometry* g, void* q, const void* p, const void* w,
+                                  double* out, int Nz, int order, void* stream);
 /* normest (gratopy.py:2366-2376): img = A^T sino with block partials of sum(img). */
 GR_API int gr_backward_sum(const gr_geometry* g, void* img, const void* sino, double* partials,
                     int Nz, int order, void* stream);
