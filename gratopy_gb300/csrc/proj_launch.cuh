@@ -4,7 +4,7 @@
 #pragma once
 
 #include "gr_internal.cuh"
-#include "projection.cuh"
+#include "projection_fast.cuh"
 
 namespace gr {
 namespace launch {
@@ -79,7 +79,11 @@ inline int clamp_split(const gr_geometry* g, int sp) {
 
 inline int fwd_split(const gr_geometry* g, int Nz) {
   if (valid_split(g->fwd_split)) return clamp_split(g, g->fwd_split);
-  const int64_t work = (int64_t)g->Ns * g->Na * ((Nz + zblock(Nz) - 1) / zblock(Nz));
+  // float32 forward: 8 lanes per group of bins measured fastest on GB300 at
+  // every size tried (256^2 .. 1200^2, single slices and 16-slice stacks).
+  if (g->dtype == GR_F32) return 8;
+  const int group = g->dtype == GR_F32 ? fast::kRayGroup : 1;
+  const int64_t work = (int64_t)g->Ns * g->Na * ((Nz + zblock(Nz) - 1) / zblock(Nz)) / group;
   const int64_t want = 2 * device_capacity();
   for (int sp = 1; sp < 8; sp <<= 1)
     if (work * sp >= want) return clamp_split(g, sp);
@@ -88,8 +92,13 @@ inline int fwd_split(const gr_geometry* g, int Nz) {
 
 inline int bwd_split(const gr_geometry* g, int Nz) {
   if (valid_split(g->bwd_split)) return clamp_split(g, g->bwd_split);
+  // float32 backprojection stages detector windows per block; splitting
+  // angles over thread rows multiplies that cost and never paid off.
+  if (g->dtype == GR_F32) return 1;
   const int64_t work = (int64_t)g->Nx * g->Ny * ((Nz + zblock(Nz) - 1) / zblock(Nz));
-  const int64_t want = 2 * device_capacity();
+  // float32 tiles stage detector windows per block: splitting angles over
+  // more thread rows multiplies that cost, so one wave is enough there.
+  const int64_t want = (g->dtype == GR_F32 ? 1 : 2) * device_capacity();
   for (int sp = 1; sp < 8; sp <<= 1)
     if (work * sp >= want) return clamp_split(g, sp);
   return clamp_split(g, 8);
@@ -97,15 +106,20 @@ inline int bwd_split(const gr_geometry* g, int Nz) {
 
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   const int ZB = zblock(Nz);
-  const int per_block = (32 / split) * (kFwdBlock / 32);
+  const int group = g->dtype == GR_F32 ? fast::kRayGroup : 1;  // bins per lane group
+  const int per_block = (32 / split) * (kFwdBlock / 32) * group;
   return dim3((g->Ns + per_block - 1) / per_block, g->Na, (Nz + ZB - 1) / ZB);
 }
+
+// Pixels per thread along the slow axis of the float32 backprojection tile
+// (2 for single slices, 1 when a thread already carries 4 slices).
+inline int bwd_py(const gr_geometry*, int) { return 1; }
 
 inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
   const int ZB = zblock(Nz);
   const int fast = io == ORDER_F ? g->Nx : g->Ny;
   const int slow = io == ORDER_F ? g->Ny : g->Nx;
-  const int rows = kBwdTileSlow / split;
+  const int rows = kBwdTileSlow / split * bwd_py(g, Nz);
   return dim3((fast + kBwdTileFast - 1) / kBwdTileFast, (slow + rows - 1) / rows, (Nz + ZB - 1) / ZB);
 }
 
@@ -114,13 +128,24 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
                   const int* skip, cudaStream_t st) {
   const Dims d = dims_of(g, Nz);
   const dim3 grid = fwd_grid(g, Nz, SPLIT);
-  if (g->kind == GR_RADON) {
-    radon_fwd_kernel<T, SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
-        img, static_cast<const T*>(g->ofs), radon_geo<T>(g->geo), d, epi, partials, skip);
+  if constexpr (std::is_same<T, float>::value) {
+    if (g->kind == GR_RADON) {
+      fast::radon_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+          img, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi, partials, skip);
+    } else {
+      fast::fan_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+          img, static_cast<const float*>(g->ofs), static_cast<const float*>(g->sdpd),
+          fan_geo<float>(g->geo), d, epi, partials, skip);
+    }
   } else {
-    fan_fwd_kernel<T, SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
-        img, static_cast<const T*>(g->ofs), static_cast<const T*>(g->sdpd), fan_geo<T>(g->geo), d,
-        epi, partials, skip);
+    if (g->kind == GR_RADON) {
+      radon_fwd_kernel<T, SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+          img, static_cast<const T*>(g->ofs), radon_geo<T>(g->geo), d, epi, partials, skip);
+    } else {
+      fan_fwd_kernel<T, SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+          img, static_cast<const T*>(g->ofs), static_cast<const T*>(g->sdpd), fan_geo<T>(g->geo),
+          d, epi, partials, skip);
+    }
   }
   return check_launch();
 }
@@ -160,13 +185,25 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
   const Dims d = dims_of(g, Nz);
   const dim3 grid = bwd_grid(g, Nz, IO, SPLIT);
   const dim3 block(kBwdTileFast, kBwdTileSlow);
-  if (g->kind == GR_RADON) {
-    radon_bwd_kernel<T, IO, SO, ZB, SPLIT, Epi><<<grid, block, 0, st>>>(
-        sino, static_cast<const T*>(g->ofs), d, epi, partials, skip);
+  if constexpr (std::is_same<T, float>::value) {
+    constexpr int PY = 1;
+    if (g->kind == GR_RADON) {
+      fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, block, 0, st>>>(
+          sino, static_cast<const float*>(g->ofs), d, epi, partials, skip);
+    } else {
+      fast::fan_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, block, 0, st>>>(
+          sino, static_cast<const float*>(g->ofs), static_cast<const float*>(g->sdpd),
+          fan_geo<float>(g->geo), d, epi, partials, skip);
+    }
   } else {
-    fan_bwd_kernel<T, IO, SO, ZB, SPLIT, Epi><<<grid, block, 0, st>>>(
-        sino, static_cast<const T*>(g->ofs), static_cast<const T*>(g->sdpd), fan_geo<T>(g->geo), d,
-        epi, partials, skip);
+    if (g->kind == GR_RADON) {
+      radon_bwd_kernel<T, IO, SO, ZB, SPLIT, Epi><<<grid, block, 0, st>>>(
+          sino, static_cast<const T*>(g->ofs), d, epi, partials, skip);
+    } else {
+      fan_bwd_kernel<T, IO, SO, ZB, SPLIT, Epi><<<grid, block, 0, st>>>(
+          sino, static_cast<const T*>(g->ofs), static_cast<const T*>(g->sdpd), fan_geo<T>(g->geo),
+          d, epi, partials, skip);
+    }
   }
   return check_launch();
 }

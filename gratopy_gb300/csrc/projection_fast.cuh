@@ -1,0 +1,686 @@
+// float32 throughput kernels for the four projections.
+//
+// Same operator as projection.cuh (gratopy radon.cl / fanbeam.cl), same
+// deterministic gather structure and epilogues, restructured to issue fewer
+// instructions per pixel-angle -- the kernels are issue-bound, not memory
+// bound:
+//  * backprojection: for every chunk of kWinAngles angles the block stages,
+//    per angle, the window of kWin consecutive detector bins its pixel tile
+//    projects onto (values outside the detector are zeros, fan values are
+//    premultiplied by sdpd).  A pixel-angle then costs two 32-bit shared
+//    loads, with no bounds tests; an angle whose window does not fit (extreme
+//    magnification) falls back to direct global loads.
+//  * forward: row bounds from one fused multiply-add each, a single
+//    approximate reciprocal per candidate pixel (fan), 32-bit offsets and an
+//    unrolled candidate loop.
+// float64 keeps the reference-order kernels of projection.cuh.
+#pragma once
+
+#include "projection.cuh"
+
+namespace gr {
+namespace fast {
+
+constexpr int kWin = 128;  // staged detector bins per angle (at most)
+
+// Angles staged per pass: 32 for single slices, 16 when 4 slices are staged.
+template <int ZB>
+struct WinAngles {
+  static constexpr int value = ZB == 1 ? 32 : 16;
+};
+
+__device__ __forceinline__ float rcp_approx(float v) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+
+// ------------------------------------------------------------ backprojection
+// Block: 32 lanes along the contiguous pixel axis x 8 thread rows; ASPLIT
+// thread rows share a pixel row and take interleaved angles; each thread owns
+// PY pixels spaced kRows apart along the slow axis.
+template <int ASPLIT, int PY>
+struct Tile {
+  static constexpr int kRows = kBwdTileSlow / ASPLIT;  // pixel rows per thread layer
+  static constexpr int kSlow = kRows * PY;             // slow extent of the tile
+};
+
+// Per-angle staged record: Radon (X, Y, off - ws, w) / fan (qx, qy, ddx, ddy,
+// dx, dy, w / R, mid - ws); `ws` is the first staged bin and `wn` the number
+// of staged bins; ws == INT_MIN marks an angle whose window does not fit
+// (its record then keeps the absolute offset / detector midpoint).
+struct RadonRec {
+  float4 r;
+  int ws, wn;
+};
+struct FanRec {
+  float4 a, b;
+  int ws, wn;
+};
+
+template <int ZB>
+struct Window {
+  float v[WinAngles<ZB>::value][ZB][kWin];
+};
+
+// Stage the windows of angles [a0, a0 + na) for slices [z0, z0 + zn): one
+// warp per angle, lanes along the detector bins (coalesced for F-ordered
+// sinograms); bins outside the detector are stored as zeros.
+template <int SO, int ZB, bool FAN, class Rec>
+__device__ __forceinline__ void stage_windows(Window<ZB>& win, const Rec* rec, int na, int a0,
+                                              const float* __restrict__ sino,
+                                              const float* __restrict__ sdpd, const Dims& d,
+                                              int64_t z0, int zn) {
+  int64_t ss_, sa_, sz_;
+  sino_strides<SO>(d, ss_, sa_, sz_);
+  const int lane = threadIdx.x, warp = threadIdx.y;
+  for (int j = warp; j < na; j += kBwdTileSlow) {
+    const int w0 = rec[j].ws, wn = rec[j].wn;
+    if (w0 == INT_MIN) continue;
+    const float* prow = sino + (int64_t)(a0 + j) * sa_ + z0 * sz_;
+    for (int k = lane; k < wn; k += 32) {
+      const int bin = w0 + k;
+      const bool in = bin >= 0 && bin < (int)d.Ns;
+      const float sc = (FAN && in) ? ldg(sdpd + bin) : 1.0f;
+      const float* p = prow + (int64_t)bin * ss_;
+#pragma unroll
+      for (int zz = 0; zz < ZB; ++zz)
+        win.v[j][zz][k] = (in && zz < zn) ? sc * ldg(p + zz * sz_) : 0.0f;
+    }
+  }
+}
+
+template <int IO, int SO, int ZB, int ASPLIT, int PY, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+radon_bwd_fast(const float* __restrict__ sino, const float* __restrict__ ofs, Dims d, Epi epi,
+               double* __restrict__ partials, const int* __restrict__ skip) {
+  using TL = Tile<ASPLIT, PY>;
+  constexpr int kWinAngles = WinAngles<ZB>::value;
+  __shared__ RadonRec rec[kWinAngles];
+  __shared__ Window<ZB> win;
+  __shared__ double red[kBwdTileFast * kBwdTileSlow / 32];
+  if (skip != nullptr && *skip) return;
+  const int g = threadIdx.y % ASPLIT;
+  const int64_t f0 = (int64_t)blockIdx.x * kBwdTileFast;
+  const int64_t s0 = (int64_t)blockIdx.y * TL::kSlow;
+  const int64_t fast = f0 + threadIdx.x;
+  const int64_t slow0 = s0 + threadIdx.y / ASPLIT;
+  const int64_t z0 = (int64_t)blockIdx.z * ZB;
+  const int zn = (int)min((int64_t)ZB, d.Nz - z0);
+  // tile corners in (x, y)
+  const float fx0 = (float)(IO == ORDER_F ? f0 : s0);
+  const float fy0 = (float)(IO == ORDER_F ? s0 : f0);
+  const float fx1 = fx0 + (float)((IO == ORDER_F ? kBwdTileFast : TL::kSlow) - 1);
+  const float fy1 = fy0 + (float)((IO == ORDER_F ? TL::kSlow : kBwdTileFast) - 1);
+  int64_t ss_, sa_, sz_;
+  sino_strides<SO>(d, ss_, sa_, sz_);
+  const int Ns = (int)d.Ns;
+  float acc[PY][ZB];
+#pragma unroll
+  for (int p = 0; p < PY; ++p)
+#pragma unroll
+    for (int k = 0; k < ZB; ++k) acc[p][k] = 0.0f;
+  const int tid = threadIdx.x + kBwdTileFast * threadIdx.y;
+  float cxs[PY], cys[PY];
+#pragma unroll
+  for (int p = 0; p < PY; ++p) {
+    const int64_t slow = slow0 + p * TL::kRows;
+    cxs[p] = (float)(IO == ORDER_F ? fast : slow);
+    cys[p] = (float)(IO == ORDER_F ? slow : fast);
+  }
+  for (int a0 = 0; a0 < d.Na; a0 += kWinAngles) {
+    const int na = (int)min((int64_t)kWinAngles, d.Na - a0);
+    __syncthreads();
+    if (tid < na) {
+      const float* o = ofs + 8 * (int64_t)(a0 + tid);
+      const float X = o[0], Y = o[1], off = o[2];
+      const float lo = off + fminf(fx0 * X, fx1 * X) + fminf(fy0 * Y, fy1 * Y);
+      const float hi = off + fmaxf(fx0 * X, fx1 * X) + fmaxf(fy0 * Y, fy1 * Y);
+      const bool finite = lo > -1e9f && hi < 1e9f;
+      const int w0 = finite ? (int)floorf(lo) - 1 : 0;
+      const int wn = finite ? (int)floorf(hi) + 3 - w0 : kWin + 1;
+      const bool fits = finite && wn <= kWin;
+      RadonRec r;
+      r.r = make_float4(X, Y, fits ? off - (float)w0 : off, o[4]);
+      r.ws = fits ? w0 : INT_MIN;
+      r.wn = fits ? wn : 0;
+      rec[tid] = r;
+    }
+    const int all_fit = __syncthreads_and(tid >= na || rec[tid].ws != INT_MIN);
+    stage_windows<SO, ZB, false>(win, rec, na, a0, sino, nullptr, d, z0, zn);
+    __syncthreads();
+    if (all_fit && na == kWinAngles) {
+      // common case: every window staged, no per-angle branch
+#pragma unroll 4
+      for (int jj = 0; jj < kWinAngles / ASPLIT; ++jj) {
+        const int j = g + jj * ASPLIT;
+        const float4 r = rec[j].r;
+#pragma unroll
+        for (int p = 0; p < PY; ++p) {
+          const float s = fmaf(cxs[p], r.x, fmaf(cys[p], r.y, r.z));
+          const float fl = floorf(s);
+          const float fr = s - fl;
+          const int i = min(max((int)fl, 0), kWin - 2);
+#pragma unroll
+          for (int k = 0; k < ZB; ++k) {
+            const float v0 = win.v[j][k][i], v1 = win.v[j][k][i + 1];
+            acc[p][k] = fmaf(r.w, fmaf(fr, v1 - v0, v0), acc[p][k]);
+          }
+        }
+      }
+    } else {
+    for (int j = g; j < na; j += ASPLIT) {
+      const RadonRec r = rec[j];
+#pragma unroll
+      for (int p = 0; p < PY; ++p) {
+        const float s = fmaf(cxs[p], r.r.x, fmaf(cys[p], r.r.y, r.r.z));
+        const float fl = floorf(s);
+        const float fr = s - fl;
+        if (r.ws != INT_MIN) {
+          const int i = min(max((int)fl, 0), kWin - 2);
+#pragma unroll
+          for (int k = 0; k < ZB; ++k) {
+            const float v0 = win.v[j][k][i], v1 = win.v[j][k][i + 1];
+            acc[p][k] = fmaf(r.r.w, fmaf(fr, v1 - v0, v0), acc[p][k]);
+          }
+        } else {
+          int sm = (int)fl, sp = sm + 1;
+          float wm = 1.0f - fr, wp = fr;
+          if (sm < 0 || sm >= Ns) { wm = 0.0f; sm = 0; }
+          if (sp < 0 || sp >= Ns) { wp = 0.0f; sp = 0; }
+          const float* pm = sino + (int64_t)(a0 + j) * sa_ + (int64_t)sm * ss_ + z0 * sz_;
+          const float* pp = sino + (int64_t)(a0 + j) * sa_ + (int64_t)sp * ss_ + z0 * sz_;
+#pragma unroll
+          for (int k = 0; k < ZB; ++k)
+            if (k < zn) acc[p][k] += r.r.w * (wm * ldg(pm + k * sz_) + wp * ldg(pp + k * sz_));
+        }
+      }
+    }
+    }
+  }
+  // fixed-order combination of the ASPLIT angle groups
+  if constexpr (ASPLIT > 1) {
+    __shared__ float cred[kBwdTileSlow][PY][ZB][kBwdTileFast];
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < PY; ++p)
+#pragma unroll
+      for (int k = 0; k < ZB; ++k) cred[threadIdx.y][p][k][threadIdx.x] = acc[p][k];
+    __syncthreads();
+    if (g == 0) {
+#pragma unroll
+      for (int p = 0; p < PY; ++p)
+#pragma unroll
+        for (int k = 0; k < ZB; ++k) {
+          float t = cred[threadIdx.y][p][k][threadIdx.x];
+#pragma unroll
+          for (int q = 1; q < ASPLIT; ++q) t += cred[threadIdx.y + q][p][k][threadIdx.x];
+          acc[p][k] = t;
+        }
+    }
+  }
+  double part = 0.0;
+  if (g == 0) {
+#pragma unroll
+    for (int p = 0; p < PY; ++p) {
+      const int64_t slow = slow0 + p * TL::kRows;
+      const int64_t x = IO == ORDER_F ? fast : slow;
+      const int64_t y = IO == ORDER_F ? slow : fast;
+      if (x < d.Nx && y < d.Ny) {
+#pragma unroll
+        for (int k = 0; k < ZB; ++k)
+          if (k < zn) part += epi(x, y, z0 + k, img_index<IO>(x, y, z0 + k, d), acc[p][k]);
+      }
+    }
+  }
+  if (Epi::kReduce) {
+    double t = block_sum(part, red);
+    if (tid == 0)
+      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
+  }
+}
+
+template <int IO, int SO, int ZB, int ASPLIT, int PY, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+fan_bwd_fast(const float* __restrict__ sino, const float* __restrict__ ofs,
+             const float* __restrict__ sdpd, FanGeo<float> gg, Dims d, Epi epi,
+             double* __restrict__ partials, const int* __restrict__ skip) {
+  using TL = Tile<ASPLIT, PY>;
+  constexpr int kWinAngles = WinAngles<ZB>::value;
+  __shared__ FanRec rec[kWinAngles];
+  __shared__ Window<ZB> win;
+  __shared__ double red[kBwdTileFast * kBwdTileSlow / 32];
+  if (skip != nullptr && *skip) return;
+  const int g = threadIdx.y % ASPLIT;
+  const int64_t f0 = (int64_t)blockIdx.x * kBwdTileFast;
+  const int64_t s0 = (int64_t)blockIdx.y * TL::kSlow;
+  const int64_t fast = f0 + threadIdx.x;
+  const int64_t slow0 = s0 + threadIdx.y / ASPLIT;
+  const int64_t z0 = (int64_t)blockIdx.z * ZB;
+  const int zn = (int)min((int64_t)ZB, d.Nz - z0);
+  const float fx0 = (float)(IO == ORDER_F ? f0 : s0) - gg.midx;
+  const float fy0 = (float)(IO == ORDER_F ? s0 : f0) - gg.midy;
+  const float fx1 = fx0 + (float)((IO == ORDER_F ? kBwdTileFast : TL::kSlow) - 1);
+  const float fy1 = fy0 + (float)((IO == ORDER_F ? TL::kSlow : kBwdTileFast) - 1);
+  int64_t ss_, sa_, sz_;
+  sino_strides<SO>(d, ss_, sa_, sz_);
+  const int Ns = (int)d.Ns;
+  const float R = gg.R;
+  const float R_sqr_inv = 1.0f / (R * R);
+  const float dxi_sqr_inv = 1.0f / (gg.delta_xi * gg.delta_xi);
+  float acc[PY][ZB];
+#pragma unroll
+  for (int p = 0; p < PY; ++p)
+#pragma unroll
+    for (int k = 0; k < ZB; ++k) acc[p][k] = 0.0f;
+  const int tid = threadIdx.x + kBwdTileFast * threadIdx.y;
+  float pxs[PY], pys[PY];
+#pragma unroll
+  for (int p = 0; p < PY; ++p) {
+    const int64_t slow = slow0 + p * TL::kRows;
+    pxs[p] = (float)(IO == ORDER_F ? fast : slow) - gg.midx;
+    pys[p] = (float)(IO == ORDER_F ? slow : fast) - gg.midy;
+  }
+  for (int a0 = 0; a0 < d.Na; a0 += kWinAngles) {
+    const int na = (int)min((int64_t)kWinAngles, d.Na - a0);
+    __syncthreads();
+    if (tid < na) {
+      const float* o = ofs + 8 * (int64_t)(a0 + tid);
+      const float qx = o[2], qy = o[3];
+      const float ddx = (o[4] - o[2]) * R_sqr_inv, ddy = (o[5] - o[3]) * R_sqr_inv;
+      const float dx = o[0] * dxi_sqr_inv, dy = o[1] * dxi_sqr_inv;
+      // projected detector coordinate of the four tile corners (a projective
+      // map: its extremes over the rectangle are at the corners)
+      float lo = 3.0e38f, hi = -3.0e38f;
+      bool ok = true;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float px = ((c & 1) ? fx1 : fx0) - qx, py = ((c & 2) ? fy1 : fy0) - qy;
+        const float t = ddx * px + ddy * py;
+        ok = ok && t > 0.0f;
+        const float xi = (dx * px + dy * py) / t + gg.mid_det;
+        lo = fminf(lo, xi);
+        hi = fmaxf(hi, xi);
+      }
+      const bool finite = ok && lo > -1e9f && hi < 1e9f;
+      const int w0 = finite ? (int)floorf(lo) - 1 : 0;
+      const int wn = finite ? (int)floorf(hi) + 3 - w0 : kWin + 1;
+      const bool fits = finite && wn <= kWin;
+      FanRec r;
+      r.a = make_float4(qx, qy, ddx, ddy);
+      r.b = make_float4(dx, dy, o[6] / R, fits ? gg.mid_det - (float)w0 : gg.mid_det);
+      r.ws = fits ? w0 : INT_MIN;
+      r.wn = fits ? wn : 0;
+      rec[tid] = r;
+    }
+    const int all_fit = __syncthreads_and(tid >= na || rec[tid].ws != INT_MIN);
+    stage_windows<SO, ZB, true>(win, rec, na, a0, sino, sdpd, d, z0, zn);
+    __syncthreads();
+    if (all_fit && na == kWinAngles) {
+#pragma unroll 4
+      for (int jj = 0; jj < kWinAngles / ASPLIT; ++jj) {
+        const int j = g + jj * ASPLIT;
+        const float4 ra = rec[j].a, rb = rec[j].b;
+#pragma unroll
+        for (int p = 0; p < PY; ++p) {
+          const float px = pxs[p] - ra.x, py = pys[p] - ra.y;
+          const float t = fmaf(ra.z, px, ra.w * py);
+          const float ss = fmaf(rb.x, px, rb.y * py);
+          const float inv = rcp_approx(t);
+          const float xi = fmaf(ss, inv, rb.w);
+          const float scale = rb.z * inv;
+          const float fl = floorf(xi);
+          const float fr = xi - fl;
+          const int i = min(max((int)fl, 0), kWin - 2);
+#pragma unroll
+          for (int k = 0; k < ZB; ++k) {
+            const float v0 = win.v[j][k][i], v1 = win.v[j][k][i + 1];
+            acc[p][k] = fmaf(scale, fmaf(fr, v1 - v0, v0), acc[p][k]);
+          }
+        }
+      }
+    } else {
+    for (int j = g; j < na; j += ASPLIT) {
+      const FanRec r = rec[j];
+#pragma unroll
+      for (int p = 0; p < PY; ++p) {
+        const float px = pxs[p] - r.a.x;
+        const float py = pys[p] - r.a.y;
+        const float t = fmaf(r.a.z, px, r.a.w * py);
+        const float ss = fmaf(r.b.x, px, r.b.y * py);
+        const float inv = rcp_approx(t);
+        const float xi = fmaf(ss, inv, r.b.w);
+        const float scale = r.b.z * inv;
+        const float fl = floorf(xi);
+        const float fr = xi - fl;
+        if (r.ws != INT_MIN) {
+          const int i = min(max((int)fl, 0), kWin - 2);
+#pragma unroll
+          for (int k = 0; k < ZB; ++k) {
+            const float v0 = win.v[j][k][i], v1 = win.v[j][k][i + 1];
+            acc[p][k] = fmaf(scale, fmaf(fr, v1 - v0, v0), acc[p][k]);
+          }
+        } else {
+          int xim = (int)fl, xip = xim + 1;
+          float Wm = 1.0f - fr, Wp = fr;
+          if (xim < 0 || xim >= Ns) { Wm = 0.0f; xim = 0; } else { Wm *= ldg(sdpd + xim); }
+          if (xip < 0 || xip >= Ns) { Wp = 0.0f; xip = 0; } else { Wp *= ldg(sdpd + xip); }
+          const float* pm = sino + (int64_t)(a0 + j) * sa_ + (int64_t)xim * ss_ + z0 * sz_;
+          const float* pp = sino + (int64_t)(a0 + j) * sa_ + (int64_t)xip * ss_ + z0 * sz_;
+#pragma unroll
+          for (int k = 0; k < ZB; ++k)
+            if (k < zn) acc[p][k] += scale * (Wm * ldg(pm + k * sz_) + Wp * ldg(pp + k * sz_));
+        }
+      }
+    }
+    }
+  }
+  if constexpr (ASPLIT > 1) {
+    __shared__ float cred[kBwdTileSlow][PY][ZB][kBwdTileFast];
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < PY; ++p)
+#pragma unroll
+      for (int k = 0; k < ZB; ++k) cred[threadIdx.y][p][k][threadIdx.x] = acc[p][k];
+    __syncthreads();
+    if (g == 0) {
+#pragma unroll
+      for (int p = 0; p < PY; ++p)
+#pragma unroll
+        for (int k = 0; k < ZB; ++k) {
+          float t = cred[threadIdx.y][p][k][threadIdx.x];
+#pragma unroll
+          for (int q = 1; q < ASPLIT; ++q) t += cred[threadIdx.y + q][p][k][threadIdx.x];
+          acc[p][k] = t;
+        }
+    }
+  }
+  double part = 0.0;
+  if (g == 0) {
+#pragma unroll
+    for (int p = 0; p < PY; ++p) {
+      const int64_t slow = slow0 + p * TL::kRows;
+      const int64_t x = IO == ORDER_F ? fast : slow;
+      const int64_t y = IO == ORDER_F ? slow : fast;
+      if (x < d.Nx && y < d.Ny) {
+#pragma unroll
+        for (int k = 0; k < ZB; ++k)
+          if (k < zn) part += epi(x, y, z0 + k, img_index<IO>(x, y, z0 + k, d), acc[p][k]);
+      }
+    }
+  }
+  if (Epi::kReduce) {
+    double t = block_sum(part, red);
+    if (tid == 0)
+      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
+  }
+}
+
+// -------------------------------------------------------------- forward
+// A thread group of SPLIT lanes owns kRayGroup adjacent detector bins of one
+// angle: the row bounds, the reciprocal (fan) and the image load of every
+// candidate pixel are shared by the group's bins, and each bin keeps its own
+// accumulator.  Candidate pixels are those between the rays through the bins
+// s0 - 1 and s0 + kRayGroup; a bin's weight is clamped at zero outside its
+// own pair of neighbouring rays, which selects exactly the pixels the
+// reference's per-ray bounds select.  Rows whose candidate range misses the
+// image are skipped by solving the two linear bound conditions for the rows.
+constexpr int kRayGroup = 4;
+
+template <int SPLIT>
+struct GroupLayout {
+  static constexpr int kGroupsPerWarp = 32 / SPLIT;
+  static constexpr int kRaysPerBlock = kGroupsPerWarp * kRayGroup * (kFwdBlock / 32);
+  int64_t s0;
+  int lane_group;
+  __device__ __forceinline__ GroupLayout() {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    s0 = (int64_t)blockIdx.x * kRaysPerBlock +
+         ((int64_t)warp * kGroupsPerWarp + lane % kGroupsPerWarp) * kRayGroup;
+    lane_group = lane / kGroupsPerWarp;
+  }
+};
+
+// Rows y in [0, n) with lo(y) = a_lo + b_lo*y <= hi_lim and
+// hi(y) = a_hi + b_hi*y >= 0 (a conservative superset: one row of margin).
+__device__ __forceinline__ void row_range(float a_lo, float b_lo, float a_hi, float b_hi,
+                                          float hi_lim, int n, int& y0, int& y1) {
+  float lo = 0.0f, hi = (float)(n - 1);
+  // a_lo + b_lo*y <= hi_lim
+  if (fabsf(b_lo) > 1e-20f) {
+    const float yb = (hi_lim - a_lo) / b_lo;
+    if (b_lo > 0.0f) hi = fminf(hi, yb); else lo = fmaxf(lo, yb);
+  } else if (a_lo > hi_lim + 1.0f) {
+    hi = -1.0f;
+  }
+  // a_hi + b_hi*y >= 0
+  if (fabsf(b_hi) > 1e-20f) {
+    const float yb = -a_hi / b_hi;
+    if (b_hi > 0.0f) lo = fmaxf(lo, yb); else hi = fminf(hi, yb);
+  } else if (a_hi < -1.0f) {
+    hi = -1.0f;
+  }
+  if (!(lo <= hi)) {  // also catches NaN bounds: then visit every row
+    if (lo == lo && hi == hi) { y0 = 0; y1 = -1; return; }
+    y0 = 0; y1 = n - 1; return;
+  }
+  y0 = max(0, (int)floorf(lo) - 1);
+  y1 = min(n - 1, (int)ceilf(hi) + 1);
+}
+
+template <int SO, int IO, int ZB, int SPLIT, class Epi>
+__global__ void __launch_bounds__(kFwdBlock)
+radon_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs, RadonGeo<float> g,
+               Dims d, Epi epi, double* __restrict__ partials, const int* __restrict__ skip) {
+  __shared__ double red[kFwdBlock / 32];
+  if (skip != nullptr && *skip) return;
+  const GroupLayout<SPLIT> L;
+  const int64_t s0 = L.s0;
+  const int64_t a = blockIdx.y;
+  const int64_t z0 = (int64_t)blockIdx.z * ZB;
+  const bool active = s0 < d.Ns;
+  const int zn = (int)min((int64_t)ZB, d.Nz - z0);
+  float acc[kRayGroup][ZB];
+#pragma unroll
+  for (int r = 0; r < kRayGroup; ++r)
+#pragma unroll
+    for (int k = 0; k < ZB; ++k) acc[r][k] = 0.0f;
+  if (active) {
+    const float* o8 = ofs + 8 * a;
+    float ox = o8[0], oy = o8[1];
+    const float oz = o8[2], ow = o8[3];
+    const bool flip = o8[5] != 0.0f;
+    int Nxx = (int)d.Nx, Nyy = (int)d.Ny;
+    int64_t sx, sy, sz;
+    img_strides<IO>(d, sx, sy, sz);
+    int64_t step_x = sx, step_y = sy;
+    if (flip) {
+      float t = ox; ox = oy; oy = t;
+      Nxx = (int)d.Ny;
+      Nyy = (int)d.Nx;
+      step_x = sy;
+      step_y = sx;
+    }
+    // position of pixel x in row y relative to bin s0: p = x*ox + dd,
+    // dd = y*oy + oz - s0; candidates have p in (-1, kRayGroup)
+    const float c_lo = ow < 0.0f ? (float)kRayGroup : -1.0f;
+    const float c_hi = ow < 0.0f ? -1.0f : (float)kRayGroup;
+    const float base = oz - (float)(int)s0;
+    // rows where the candidate x-range meets [0, Nxx-1]
+    const float lx = (float)(Nxx - 1) * ox;
+    int y0, y1;
+    row_range(base + fminf(0.0f, lx) - (float)kRayGroup, oy, base + fmaxf(0.0f, lx) + 1.0f, oy,
+              0.0f, Nyy, y0, y1);
+    const float* img0 = img + z0 * sz;
+    const int ys = y0 + L.lane_group;
+    float yf = (float)ys;
+    for (int y = ys; y <= y1; y += SPLIT, yf += (float)SPLIT) {
+      const float dd = fmaf(yf, oy, base);
+      const int x_low = max((int)((c_lo - dd) * ow), 0);
+      const int x_high = min((int)((c_hi - dd) * ow), Nxx - 1);
+      const float* p = img0 + (int64_t)y * step_y + (int64_t)x_low * step_x;
+      float pos = fmaf((float)x_low, ox, dd);
+      for (int x = x_low; x <= x_high; ++x) {
+        float v[ZB];
+#pragma unroll
+        for (int k = 0; k < ZB; ++k) v[k] = k < zn ? ldg(p + k * sz) : 0.0f;
+#pragma unroll
+        for (int r = 0; r < kRayGroup; ++r) {
+          const float w = 1.0f - fabsf(pos - (float)r);
+          if (w > 0.0f) {
+#pragma unroll
+            for (int k = 0; k < ZB; ++k) acc[r][k] = fmaf(w, v[k], acc[r][k]);
+          }
+        }
+        pos += ox;
+        p += step_x;
+      }
+    }
+  }
+  if (SPLIT > 1) {
+#pragma unroll
+    for (int r = 0; r < kRayGroup; ++r) warp_reduce_rows<SPLIT>(acc[r]);
+  }
+  double part = 0.0;
+  if (active && L.lane_group == 0) {
+    const float scale = g.delta_x * g.delta_x / g.delta_xi;
+#pragma unroll
+    for (int r = 0; r < kRayGroup; ++r) {
+      const int64_t s = s0 + r;
+      if (s < d.Ns) {
+#pragma unroll
+        for (int k = 0; k < ZB; ++k)
+          if (k < zn) part += epi(s, a, z0 + k, sino_index<SO>(s, a, z0 + k, d), acc[r][k] * scale);
+      }
+    }
+  }
+  if (Epi::kReduce) {
+    double t = block_sum(part, red);
+    if (threadIdx.x == 0)
+      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
+  }
+}
+
+template <int SO, int IO, int ZB, int SPLIT, class Epi>
+__global__ void __launch_bounds__(kFwdBlock)
+fan_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs,
+             const float* __restrict__ sdpd, FanGeo<float> g, Dims d, Epi epi,
+             double* __restrict__ partials, const int* __restrict__ skip) {
+  __shared__ double red[kFwdBlock / 32];
+  if (skip != nullptr && *skip) return;
+  const GroupLayout<SPLIT> L;
+  const int64_t s0 = L.s0;
+  const int64_t a = blockIdx.y;
+  const int64_t z0 = (int64_t)blockIdx.z * ZB;
+  const bool active = s0 < d.Ns;
+  const int zn = (int)min((int64_t)ZB, d.Nz - z0);
+  float acc[kRayGroup][ZB];
+#pragma unroll
+  for (int r = 0; r < kRayGroup; ++r)
+#pragma unroll
+    for (int k = 0; k < ZB; ++k) acc[r][k] = 0.0f;
+  const float R = g.R;
+  if (active) {
+    float midx = g.midx, midy = g.midy;
+    const float* o = ofs + 8 * a;
+    float dx = o[0], dy = o[1], qx = o[2], qy = o[3];
+    const float d0x = o[4], d0y = o[5];
+    const float sr = (float)(int)s0;
+    // boundary rays of the group: through bins s0 - 1 and s0 + kRayGroup
+    const float fp = -g.mid_det + sr + (float)kRayGroup;
+    const float fm = -g.mid_det + sr - 1.0f;
+    float dpx = d0x + dx * fp - qx, dpy = d0y + dy * fp - qy;
+    float dmx = d0x + dx * fm - qx, dmy = d0y + dy * fm - qy;
+    float ddx = (d0x - qx) / (R * R), ddy = (d0y - qy) / (R * R);
+    const float xx2 = g.delta_xi * g.delta_xi;
+    dx /= xx2;
+    dy /= xx2;
+    const float RE = g.RE * (1.0f / R);
+    int Nyy = (int)d.Ny, Nxx = (int)d.Nx;
+    int64_t sx, sy, sz;
+    img_strides<IO>(d, sx, sy, sz);
+    int64_t step_x = sx, step_y = sy;
+    if (!(fabsf(dpx) < fabsf(dpy) && fabsf(dmx) < fabsf(dmy))) {
+      float t;
+      t = ddx; ddx = ddy; ddy = t;
+      t = dx; dx = dy; dy = t;
+      t = qx; qx = qy; qy = t;
+      t = dpx; dpx = dpy; dpy = t;
+      t = dmx; dmx = dmy; dmy = t;
+      t = midx; midx = midy; midy = t;
+      Nyy = (int)d.Nx;
+      Nxx = (int)d.Ny;
+      step_x = sy;
+      step_y = sx;
+    }
+    dpx /= dpy;
+    dmx /= dmy;
+    if (qy * (dmx - dpx) < 0.0f) {
+      float t = dpx; dpx = dmx; dmx = t;
+    }
+    const float s_mid0 = sr - g.mid_det;
+    // row y: candidate x (absolute pixel index) in
+    // [ceil(qxm + dmx*yrel), floor(qxm + dpx*yrel)], yrel = y - midy - qy
+    const float qxm = qx + midx, yc = -midy - qy;
+    const float hi_lim = (float)(Nxx - 1);
+    const float t_c = RE - ddx * midx - ddy * midy;
+    const float s_c = -dx * midx - dy * midy;
+    int y0, y1;
+    row_range(fmaf(dmx, yc, qxm), dmx, fmaf(dpx, yc, qxm), dpx, hi_lim, Nyy, y0, y1);
+    const float* img0 = img + z0 * sz;
+    const int ys = y0 + L.lane_group;
+    float yf = (float)ys;
+    for (int y = ys; y <= y1; y += SPLIT, yf += (float)SPLIT) {
+      const float yrel = yf + yc;
+      const int xhi = (int)floorf(fminf(hi_lim, fmaf(dpx, yrel, qxm)));
+      const int xlo = (int)ceilf(fmaxf(0.0f, fmaf(dmx, yrel, qxm)));
+      const float xlf = (float)xlo;
+      float t = fmaf(ddx, xlf, fmaf(ddy, yf, t_c));
+      float ss = fmaf(dx, xlf, fmaf(dy, yf, s_c));
+      const float* p = img0 + (int64_t)y * step_y + (int64_t)xlo * step_x;
+      for (int x = xlo; x <= xhi; ++x) {
+        const float r = rcp_approx(t);
+        const float u = fmaf(ss, r, -s_mid0);  // xi - (s0 - mid) in bins
+        float v[ZB];
+#pragma unroll
+        for (int k = 0; k < ZB; ++k) v[k] = k < zn ? ldg(p + k * sz) * r : 0.0f;
+#pragma unroll
+        for (int q = 0; q < kRayGroup; ++q) {
+          const float w = 1.0f - fabsf((float)q - u);
+          if (w > 0.0f) {
+#pragma unroll
+            for (int k = 0; k < ZB; ++k) acc[q][k] = fmaf(w, v[k], acc[q][k]);
+          }
+        }
+        p += step_x;
+        t += ddx;
+        ss += dx;
+      }
+    }
+  }
+  if (SPLIT > 1) {
+#pragma unroll
+    for (int r = 0; r < kRayGroup; ++r) warp_reduce_rows<SPLIT>(acc[r]);
+  }
+  double part = 0.0;
+  if (active && L.lane_group == 0) {
+#pragma unroll
+    for (int q = 0; q < kRayGroup; ++q) {
+      const int64_t s = s0 + q;
+      if (s < d.Ns) {
+        const float sc = sdpd[s] / g.delta_xi * g.delta_x / R;
+#pragma unroll
+        for (int k = 0; k < ZB; ++k)
+          if (k < zn) part += epi(s, a, z0 + k, sino_index<SO>(s, a, z0 + k, d), acc[q][k] * sc);
+      }
+    }
+  }
+  if (Epi::kReduce) {
+    double t = block_sum(part, red);
+    if (threadIdx.x == 0)
+      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
+  }
+}
+
+}  // namespace fast
+}  // namespace gr
