@@ -64,6 +64,11 @@ SIGNATURES = {
     "gr_backward_cg": (_I, [_G, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "gr_backward_sum": (_I, [_G, _P, _P, _P, _I, _I, _P]),
     "gr_forward_wsq_noalloc": (_I, [_G, _P, _P, _P, _P, _I, _I, _P]),
+    "gr_forward_angle_axpy": (_I, [_G, _P, _P, _P, _P, _D, _I, _I, _P]),
+    "gr_backward_tv_adjoint": (_I, [_G, _P, _P, _P, _F, _F, _F, _I, _I, _P]),
+    "gr_tv_adjoint_primal": (_I, [_P, _P, _P, _P, _P, _I, _Z, _P]),
+    "gr_tv_adjoint_dual": (_I, [_P, _P, _P, _P, _P, _F, _F, _F, _I, _I, _I, _I, _I, _P]),
+    "gr_tv_adjoint_lambda": (_I, [_P, _P, _P, _F, _F, _I, _Z, _P]),
     "gr_forward_partials": (_Z, [_G, _I]),
     "gr_backward_partials": (_Z, [_G, _I, _I]),
     "gr_weight_sinogram": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),

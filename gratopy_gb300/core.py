@@ -190,6 +190,7 @@ class ProjectionSettings:
         self.buf_upload = {}
         self._dev = {}
         self._geom = {}
+        self._geom_adj = {}
 
         if self.reverse_detector and self.is_parallel:
             print(
@@ -305,6 +306,11 @@ class ProjectionSettings:
         if self.is_fan:
             tables["sdpd"] = torch.from_numpy(
                 np.asarray(self.struct["sdpd_dict"][dtype]).reshape(-1)).to(dev, tdt)
+        # table of the plain transpose A^T: the angle-weight column replaced
+        # by the forward projection's scale
+        adj = np.array(ofs, copy=True)
+        adj[:, 6 if self.is_fan else 4] = self.forward_scale(dtype)
+        tables["ofs_adj"] = torch.from_numpy(adj.reshape(-1)).to(dev, tdt)
         self._dev[dtype] = tables
         self.buf_upload[dtype] = 1
         g = _lib.GrGeometry()
@@ -318,6 +324,24 @@ class ProjectionSettings:
         for i, v in enumerate(geo):
             g.geo[i] = float(v)
         self._geom[dtype] = g
+        ga = _lib.GrGeometry.from_buffer_copy(g)
+        ga.ofs = tables["ofs_adj"].data_ptr()
+        self._geom_adj[dtype] = ga
+
+    def forward_scale(self, dtype) -> float:
+        """Scale the forward kernels apply after the interpolation sums, in their arithmetic.
+
+        Radon: dx*dx/ds with dx, ds rounded to float32 (radon.cl:82-83,160);
+        fan beam: dx/(ds/dx) (fanbeam.cl:254-255, with sdpd[s]/R applied per bin).
+        A^T is the backprojection with this value as every angle weight.
+        """
+        dtype = _np_dtype(dtype)
+        geo = np.asarray(self.struct["geo_dict"][dtype])
+        if self.is_fan:
+            return float(dtype.type(geo[10]) / dtype.type(geo[2]))
+        dx = dtype.type(np.float32(geo[0]))
+        ds = dtype.type(np.float32(geo[1]))
+        return float(dx * dx / ds)
 
     def device_tables(self, dtype) -> dict:
         self.ensure_dtype(dtype)
@@ -327,6 +351,11 @@ class ProjectionSettings:
         """C-ABI geometry descriptor for precision ``dtype`` (tables uploaded)."""
         self.ensure_dtype(dtype)
         return self._geom[_np_dtype(dtype)]
+
+    def gr_geometry_adjoint(self, dtype) -> _lib.GrGeometry:
+        """Descriptor whose backprojection is the plain transpose of the forward projection."""
+        self.ensure_dtype(dtype)
+        return self._geom_adj[_np_dtype(dtype)]
 
     def set_angle_weights(self, angle_weights) -> None:
         """Replace the angle weights and re-upload the tables (gratopy.py:1697-1756)."""
@@ -349,6 +378,7 @@ class ProjectionSettings:
         uploaded = list(self._dev.keys())
         self._dev.clear()
         self._geom.clear()
+        self._geom_adj.clear()
         for dtype in uploaded:
             self.ensure_dtype(dtype)
 
@@ -602,19 +632,50 @@ class _Scratch:
         return ctypes.c_void_p(self.sc.data_ptr() + 8 * k)
 
 
+GRAPH_CHUNK = 25
+
+
+def _iterate(body, n: int, device, use_graph: bool) -> None:
+    """Run ``body()`` ``n`` times on the current stream.
+
+    With ``use_graph`` the launches of up to GRAPH_CHUNK iterations are
+    captured once into a CUDA graph and the graph is replayed; the remainder
+    runs directly.  ``body`` must launch the same kernels with the same
+    arguments every iteration and must not allocate or synchronise.
+    """
+    if n <= 0:
+        return
+    if not use_graph or n < 2 or torch.cuda.is_current_stream_capturing():
+        for _ in range(n):
+            body()
+        return
+    chunk = min(n, GRAPH_CHUNK)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        for _ in range(chunk):
+            body()
+    reps, rem = divmod(n, chunk)
+    for _ in range(reps):
+        graph.replay()
+    for _ in range(rem):
+        body()
+
+
 def _dot_into(scr: _Scratch, slot: int, a, b, stream) -> None:
     _lib.call("gr_dot_partials", _ptr(scr.dot), _ptr(a), _ptr(b), _dt(a), a.numel(), stream)
     _lib.call("gr_sum_partials", scr.slot(slot), _ptr(scr.dot), scr.dot.numel(), stream)
 
 
-def normest(projectionsetting, number_iterations=50, dtype="float32", allocator=None, x0=None):
+def normest(projectionsetting, number_iterations=50, dtype="float32", allocator=None, x0=None,
+            use_graph=True):
     """Spectral-norm estimate by power iteration (gratopy.py:2329-2377).
 
     The iterate is normalised by its plain sum (not its norm) before each
     application of A^T A, as in the reference; the sum is a float64 device
-    reduction and the whole loop runs without host synchronisation.  The
-    start vector is ``np.random.randn`` (seed numpy's global generator to
-    reproduce it) unless ``x0`` is given.
+    reduction and the whole loop runs without host synchronisation (captured
+    in a CUDA graph unless ``use_graph=False``).  The start vector is
+    ``np.random.randn`` (seed numpy's global generator to reproduce it)
+    unless ``x0`` is given.
     """
     ps = projectionsetting
     if number_iterations < 1:
@@ -636,15 +697,21 @@ def normest(projectionsetting, number_iterations=50, dtype="float32", allocator=
         n_bwd = int(_lib.raw("gr_backward_partials")(ctypes.byref(g), 1, _lib.GR_ORDER_F))
         scr = _Scratch(dev, n_bwd)
         n = img.numel()
+        # the sum of the start vector goes into partial 0 (the others are 0),
+        # so every iteration starts by summing the same partials buffer
+        scr.part.zero_()
         _lib.call("gr_sum_values_partials", _ptr(scr.dot), _ptr(img), _dt(img), n, st)
-        _lib.call("gr_sum_partials", scr.slot(_lib.SC_SUM), _ptr(scr.dot), scr.dot.numel(), st)
-        for i in range(number_iterations):
-            _lib.call("gr_scale_by_sum", _ptr(img), _ptr(scr.sc), _dt(img), n, st)
-            _lib.call("gr_forward", ctypes.byref(g), _ptr(sino), _ptr(img), 1, 0, 0, st)
-            _lib.call("gr_backward_sum", ctypes.byref(g), _ptr(img), _ptr(sino), _ptr(scr.part), 1,
-                      0, st)
-            if i < number_iterations - 1:
-                _lib.call("gr_sum_partials", scr.slot(_lib.SC_SUM), _ptr(scr.part), n_bwd, st)
+        _lib.call("gr_sum_partials", _ptr(scr.part), _ptr(scr.dot), scr.dot.numel(), st)
+        gptr = ctypes.byref(g)
+
+        def body():
+            s_ = _stream_ptr(dev)
+            _lib.call("gr_sum_partials", scr.slot(_lib.SC_SUM), _ptr(scr.part), n_bwd, s_)
+            _lib.call("gr_scale_by_sum", _ptr(img), _ptr(scr.sc), _dt(img), n, s_)
+            _lib.call("gr_forward", gptr, _ptr(sino), _ptr(img), 1, 0, 0, s_)
+            _lib.call("gr_backward_sum", gptr, _ptr(img), _ptr(sino), _ptr(scr.part), 1, 0, s_)
+
+        _iterate(body, number_iterations, dev, use_graph)
         normsqr = float(scr.sc[_lib.SC_SUM].item())
     return float(np.sqrt(normsqr))
 
@@ -653,7 +720,8 @@ def _img_shape_for(sino, ps):
     return tuple(ps.img_shape) + ((int(sino.shape[2]),) if sino.dim() > 2 else ())
 
 
-def landweber(sino, projectionsetting, number_iterations=100, w=1.0, norm_estimate=None):
+def landweber(sino, projectionsetting, number_iterations=100, w=1.0, norm_estimate=None,
+              use_graph=True):
     """Landweber (SIRT) iteration (gratopy.py:2380-2446).
 
     Each iteration is two fused launches: r = A u - f, then u += -w' A^T r
@@ -672,19 +740,21 @@ def landweber(sino, projectionsetting, number_iterations=100, w=1.0, norm_estima
     resid = empty(sino.shape, sino.dtype, order, dev)
     unew = zeros(_img_shape_for(sino, ps), sino.dtype, order, dev)
     of = _oflag(order)
-    with torch.cuda.device(dev):
+    gptr = ctypes.byref(g)
+
+    def body():
         st = _stream_ptr(dev)
-        for i in range(number_iterations):
-            _progress("\rProgress at {:3.0%}".format(float(i) / number_iterations))
-            _lib.call("gr_forward_residual", ctypes.byref(g), _ptr(resid), _ptr(unew), _ptr(sino),
-                      Nz, of, st)
-            _lib.call("gr_backward_axpy", ctypes.byref(g), _ptr(unew), _ptr(resid), float(-wq), Nz,
-                      of, st)
+        _lib.call("gr_forward_residual", gptr, _ptr(resid), _ptr(unew), _ptr(sino), Nz, of, st)
+        _lib.call("gr_backward_axpy", gptr, _ptr(unew), _ptr(resid), float(-wq), Nz, of, st)
+
+    with torch.cuda.device(dev):
+        _iterate(body, number_iterations, dev, use_graph)
     _progress("\rLandweber reconstruction complete\n")
     return unew
 
 
-def conjugate_gradients(sino, projectionsetting, number_iterations=20, epsilon=0.0, x0=None):
+def conjugate_gradients(sino, projectionsetting, number_iterations=20, epsilon=0.0, x0=None,
+                        use_graph=True):
     """CG on the normal equations in gratopy's weighted inner products (gratopy.py:2449-2551).
 
     Step sizes stay on the device (float64 reductions, no host round trip);
@@ -724,26 +794,30 @@ def conjugate_gradients(sino, projectionsetting, number_iterations=20, epsilon=0
         _lib.call("gr_backward", ctypes.byref(g), _ptr(p), _ptr(d), Nz, of, of, st)
         _dot_into(scr, _lib.SC_SOLD, p, p, st)
         _dot_into(scr, _lib.SC_FSQ, sino, sino, st)
-        for k in range(number_iterations):
-            _progress("\rProgress at {:3.0%}".format(float(k) / number_iterations))
-            _lib.call("gr_forward_wsq", ctypes.byref(g), _ptr(q), _ptr(p), _ptr(t["w"]),
-                      _ptr(scr.part), _ptr(scr.done), Nz, of, st)
+        gptr = ctypes.byref(g)
+
+        def body():
+            st_ = _stream_ptr(dev)
+            _lib.call("gr_forward_wsq", gptr, _ptr(q), _ptr(p), _ptr(t["w"]),
+                      _ptr(scr.part), _ptr(scr.done), Nz, of, st_)
             _lib.call("gr_cg_alpha", _ptr(scr.sc), _ptr(scr.part), n_fwd, float(c), _dt(sino),
-                      _ptr(scr.done), st)
+                      _ptr(scr.done), st_)
             _lib.call("gr_cg_update_d", _ptr(d), _ptr(q), _ptr(scr.sc), _ptr(scr.dot), _dt(sino),
-                      d.numel(), _ptr(scr.done), st)
-            _lib.call("gr_backward_cg", ctypes.byref(g), _ptr(snew), _ptr(d), _ptr(x), _ptr(p),
-                      scr.slot(_lib.SC_ALPHA), _ptr(scr.part2), _ptr(scr.done), Nz, of, st)
+                      d.numel(), _ptr(scr.done), st_)
+            _lib.call("gr_backward_cg", gptr, _ptr(snew), _ptr(d), _ptr(x), _ptr(p),
+                      scr.slot(_lib.SC_ALPHA), _ptr(scr.part2), _ptr(scr.done), Nz, of, st_)
             _lib.call("gr_cg_beta", _ptr(scr.sc), _ptr(scr.part2), n_bwd, _ptr(scr.dot), n_dot,
-                      float(epsilon), _dt(sino), _ptr(scr.done), st)
+                      float(epsilon), _dt(sino), _ptr(scr.done), st_)
             _lib.call("gr_cg_update_p", _ptr(p), _ptr(snew), _ptr(scr.sc), _dt(sino), p.numel(),
-                      _ptr(scr.done), st)
+                      _ptr(scr.done), st_)
+
+        _iterate(body, number_iterations, dev, use_graph)
     _progress("\rCG reconstruction complete\n")
     return x
 
 
 def total_variation(sino, projectionsetting, mu, number_iterations=1000, slice_thickness=1.0,
-                    stepsize_weighting=10.0, norm_estimate=None):
+                    stepsize_weighting=10.0, norm_estimate=None, use_graph=True):
     """L2-TV primal-dual (Chambolle-Pock) reconstruction (gratopy.py:2554-2762).
 
     Per iteration three launches: the fused dual step (gradient + unit-ball
@@ -780,16 +854,20 @@ def total_variation(sino, projectionsetting, mu, number_iterations=1000, slice_t
     f32 = lambda v: float(np.float32(v))  # noqa: E731  (scalars are float32 kernel args)
     of = _oflag(order)
     Nx, Ny = ps.img_shape
-    with torch.cuda.device(dev):
+    gptr = ctypes.byref(g)
+    sig, z_d = f32(sigma), f32(slice_thickness)
+    sig_l, mu_f = f32(sigma / norm_estimate), f32(mu)
+    tau_f, norming = f32(tau), f32(1.0 / norm_estimate)
+
+    def body():
         st = _stream_ptr(dev)
-        for i in range(number_iterations):
-            _lib.call("gr_tv_dual", _ptr(V), _ptr(Ubar), f32(sigma), f32(slice_thickness),
-                      _dt(sino), Nx, Ny, Nz, of, st)
-            _lib.call("gr_forward_lambda", ctypes.byref(g), _ptr(Lamb), _ptr(Ubar), _ptr(sino),
-                      f32(sigma / norm_estimate), f32(mu), Nz, of, st)
-            _lib.call("gr_backward_tv_primal", ctypes.byref(g), _ptr(U), _ptr(Ubar), _ptr(V),
-                      _ptr(Lamb), f32(tau), f32(1.0 / norm_estimate), f32(slice_thickness), Nz, of,
-                      st)
-            _progress("\rProgress at {:3.0%}".format(float(i) / number_iterations))
+        _lib.call("gr_tv_dual", _ptr(V), _ptr(Ubar), sig, z_d, _dt(sino), Nx, Ny, Nz, of, st)
+        _lib.call("gr_forward_lambda", gptr, _ptr(Lamb), _ptr(Ubar), _ptr(sino), sig_l, mu_f, Nz,
+                  of, st)
+        _lib.call("gr_backward_tv_primal", gptr, _ptr(U), _ptr(Ubar), _ptr(V), _ptr(Lamb), tau_f,
+                  norming, z_d, Nz, of, st)
+
+    with torch.cuda.device(dev):
+        _iterate(body, number_iterations, dev, use_graph)
     _progress("\rTV reconstruction complete\n")
     return U

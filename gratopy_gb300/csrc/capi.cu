@@ -135,4 +135,21 @@ int gr_backward_sum(const gr_geometry* g, void* img, const void* sino, double* p
                   bwd_sum<double>(g, img, sino, partials, Nz, order, stream));
 }
 
+int gr_forward_angle_axpy(const gr_geometry* g, void* out, const void* base, const void* u,
+                          const void* w, double c, int Nz, int order, void* stream) {
+  if (!same_order_ok(g, order) || out == nullptr || u == nullptr || w == nullptr) return GR_ERR_ARG;
+  return GR_TYPED(fwd_angle_axpy<float>(g, out, base, u, w, c, Nz, order, stream),
+                  fwd_angle_axpy<double>(g, out, base, u, w, c, Nz, order, stream));
+}
+
+int gr_backward_tv_adjoint(const gr_geometry* g, void* out, const void* lambda, const void* gw,
+                           float c1, float sigma, float z_distance, int Nz, int order,
+                           void* stream) {
+  if (!same_order_ok(g, order) || out == nullptr || lambda == nullptr || gw == nullptr)
+    return GR_ERR_ARG;
+  return GR_TYPED(
+      bwd_tv_adjoint<float>(g, out, lambda, gw, c1, sigma, z_distance, Nz, order, stream),
+      bwd_tv_adjoint<double>(g, out, lambda, gw, c1, sigma, z_distance, Nz, order, stream));
+}
+
 }  // extern "C"

@@ -14,4 +14,8 @@ template int fwd_wsq<float>(const gr_geometry*, void*, const void*, const void*,
 template int bwd_cg<float>(const gr_geometry*, void*, const void*, void*, const void*, const double*,
                         double*, const int*, int, int, void*);
 template int bwd_sum<float>(const gr_geometry*, void*, const void*, double*, int, int, void*);
+template int fwd_angle_axpy<float>(const gr_geometry*, void*, const void*, const void*, const void*,
+                                double, int, int, void*);
+template int bwd_tv_adjoint<float>(const gr_geometry*, void*, const void*, const void*, float, float,
+                                float, int, int, void*);
 }  // namespace gr

@@ -14,4 +14,8 @@ template int fwd_wsq<double>(const gr_geometry*, void*, const void*, const void*
 template int bwd_cg<double>(const gr_geometry*, void*, const void*, void*, const void*, const double*,
                         double*, const int*, int, int, void*);
 template int bwd_sum<double>(const gr_geometry*, void*, const void*, double*, int, int, void*);
+template int fwd_angle_axpy<double>(const gr_geometry*, void*, const void*, const void*, const void*,
+                                double, int, int, void*);
+template int bwd_tv_adjoint<double>(const gr_geometry*, void*, const void*, const void*, float, float,
+                                float, int, int, void*);
 }  // namespace gr

@@ -38,6 +38,12 @@ int bwd_cg(const gr_geometry* g, void* snew, const void* d, void* x, const void*
 template <typename T>
 int bwd_sum(const gr_geometry* g, void* img, const void* sino, double* partials, int Nz, int order,
             void* stream);
+template <typename T>
+int fwd_angle_axpy(const gr_geometry* g, void* out, const void* base, const void* u,
+                   const void* w, double c, int Nz, int order, void* stream);
+template <typename T>
+int bwd_tv_adjoint(const gr_geometry* g, void* out, const void* lambda, const void* gw, float c1,
+                   float sigma, float z_distance, int Nz, int order, void* stream);
 
 #ifdef GR_DEFINE_PLAIN
 template <typename T>
@@ -142,6 +148,31 @@ int bwd_sum(const gr_geometry* g, void* img, const void* sino, double* partials,
     constexpr int O = decltype(o)::value;
     return launch::launch_bwd<T, O, O>(g, sino, Nz, BwdStoreSum<T>{static_cast<T*>(img)}, partials,
                                        nullptr, stream);
+  });
+}
+
+template <typename T>
+int fwd_angle_axpy(const gr_geometry* g, void* out, const void* base, const void* u,
+                   const void* w, double c, int Nz, int order, void* stream) {
+  return dispatch_order(order, [&](auto o) {
+    constexpr int O = decltype(o)::value;
+    return launch::launch_fwd<T, O, O>(
+        g, u, Nz,
+        FwdAngleAxpy<T>{static_cast<T*>(out), static_cast<const T*>(base),
+                        static_cast<const T*>(w), (T)c},
+        nullptr, nullptr, stream);
+  });
+}
+
+template <typename T>
+int bwd_tv_adjoint(const gr_geometry* g, void* out, const void* lambda, const void* gw, float c1,
+                   float sigma, float z_distance, int Nz, int order, void* stream) {
+  const Dims d = launch::dims_of(g, Nz);
+  return dispatch_order(order, [&](auto o) {
+    constexpr int O = decltype(o)::value;
+    BwdTVAdjoint<T, O> e{static_cast<T*>(out), static_cast<const T*>(gw), d, c1, sigma,
+                         z_distance};
+    return launch::launch_bwd<T, O, O>(g, lambda, Nz, e, nullptr, nullptr, stream);
   });
 }
 #endif

@@ -172,6 +172,50 @@ struct BwdTVPrimal {
   }
 };
 
+// Transposes and the unrolled-TV adjoint.
+// out = base + c * w[a] * (A u)   (base may be null): B^T h = (ds/dx / dx) W A h
+// is this with base = null, c = ds/dx / dx; the TV adjoint uses a base.
+template <typename T>
+struct FwdAngleAxpy {
+  static constexpr bool kReduce = false;
+  T* out;
+  const T* base;
+  const T* w;
+  T c;
+  __device__ __forceinline__ double operator()(int64_t, int64_t a, int64_t, int64_t i, T v) const {
+    const T b = base ? base[i] : (T)0.;
+    out[i] = b + c * w[a] * v;
+    return 0.0;
+  }
+};
+
+// Adjoint of the TV extragradient/dual coupling on the image:
+// out = c1 * (A^T lambda_bar) - sigma * div(gw), div as in total_variation.cl:119-143.
+template <typename T, int O>
+struct BwdTVAdjoint {
+  static constexpr bool kReduce = false;
+  T* out;
+  const T* gw;
+  Dims d;
+  float c1, sigma, z_distance;
+  __device__ __forceinline__ double operator()(int64_t x, int64_t y, int64_t z, int64_t i,
+                                               T v) const {
+    int64_t sx, sy, sz;
+    img_strides<O>(d, sx, sy, sz);
+    const T* vp = gw + 4 * i;
+    T v0 = vp[0], v1 = vp[1], v2 = vp[2];
+    if (x == d.Nx - 1) v0 = (T)0.;
+    if (x > 0) v0 -= vp[-4 * sx + 0];
+    if (y == d.Ny - 1) v1 = (T)0.;
+    if (y > 0) v1 -= vp[-4 * sy + 1];
+    if (z == d.Nz - 1) v2 = (T)0.;
+    if (z > 0) v2 -= vp[-4 * sz + 2];
+    if (z_distance > 0) v2 /= z_distance; else v2 = (T)0.;
+    out[i] = c1 * v - sigma * (v0 + v1 + v2);
+    return 0.0;
+  }
+};
+
 // ------------------------------------------------------------------ helpers
 
 // Per-angle record of the Radon backprojection staged in shared memory.

@@ -130,6 +130,30 @@ GR_API int gr_backward_cg(const gr_geometry* g, void* snew, const void* d, void*
  * overlap on the GPU race. */
 GR_API int gr_forward_wsq_noalloc(const gr_geometry* g, void* q, const void* p, const void* w,
                                   double* out, int Nz, int order, void* stream);
+/* Transposes for differentiation (no counterpart in the reference, which
+ * has no gradients): out = base + c * w[a] * (A u), base may be NULL.  With
+ * c = (ds/dx)/dx and w the angle weights this is the plain transpose of
+ * gratopy's backprojection; the plain transpose of the forward projection is
+ * gr_backward with the per-angle weights of ofs replaced by dx/(ds/dx). */
+GR_API int gr_forward_angle_axpy(const gr_geometry* g, void* out, const void* base, const void* u,
+                                 const void* w, double c, int Nz, int order, void* stream);
+/* Adjoint of one TV primal-dual iteration (reverse mode through
+ * total_variation.cl:54-167): out = c1 * (A^T lambda) - sigma * div(gw) on
+ * the image, with A^T from an adjoint geometry as above. */
+GR_API int gr_backward_tv_adjoint(const gr_geometry* g, void* out, const void* lambda,
+                                  const void* gw, float c1, float sigma, float z_distance, int Nz,
+                                  int order, void* stream);
+/* Elementwise parts of the TV adjoint (csrc/tv_adjoint.cu):
+ * gz = [u_next > 0] (gu + 2 gubar), gu_prev = gz - gubar */
+GR_API int gr_tv_adjoint_primal(void* gz, void* gu_prev, const void* gu, const void* gubar,
+                                const void* u_next, int dtype, size_t n, void* stream);
+/* gw = J_P(w)^T (gv - tau grad gz), w = v + sigma grad ubar (4 reals/pixel) */
+GR_API int gr_tv_adjoint_dual(void* gw, const void* gv, const void* gz, const void* v,
+                              const void* ubar, float sigma, float tau, float z_distance, int dtype,
+                              int Nx, int Ny, int Nz, int order, void* stream);
+/* gl_prev = mu2 gl1, gf -= mu2 sigma_l gl1 (sinogram-sized) */
+GR_API int gr_tv_adjoint_lambda(void* gl_prev, void* gf, const void* gl1, float mu2, float sigma_l,
+                                int dtype, size_t n, void* stream);
 /* normest (gratopy.py:2366-2376): img = A^T sino with block partials of sum(img). */
 GR_API int gr_backward_sum(const gr_geometry* g, void* img, const void* sino, double* partials,
                     int Nz, int order, void* stream);
