@@ -38,6 +38,28 @@ class GrGeometry(ctypes.Structure):
     ]
 
 
+class GrBatchProblem(ctypes.Structure):
+    """Mirror of ``struct gr_batch_problem``."""
+
+    _fields_ = [
+        ("kind", ctypes.c_int), ("Nx", ctypes.c_int), ("Ny", ctypes.c_int),
+        ("Ns", ctypes.c_int), ("Na", ctypes.c_int), ("solver", ctypes.c_int),
+        ("fwd_split", ctypes.c_int), ("fwd_tiles_x", ctypes.c_int),
+        ("bwd_tiles_x", ctypes.c_int), ("bwd_tiles_y", ctypes.c_int),
+        ("ofs", ctypes.c_void_p), ("sdpd", ctypes.c_void_p), ("w", ctypes.c_void_p),
+        ("geo", ctypes.c_float * 8),
+        ("f", ctypes.c_void_p), ("img", ctypes.c_void_p), ("s1", ctypes.c_void_p),
+        ("s2", ctypes.c_void_p), ("i1", ctypes.c_void_p), ("i2", ctypes.c_void_p),
+        ("v4", ctypes.c_void_p), ("sc", ctypes.c_void_p), ("fwd_part", ctypes.c_void_p),
+        ("bwd_part", ctypes.c_void_p),
+        ("a0", ctypes.c_float), ("a1", ctypes.c_float), ("a2", ctypes.c_float),
+        ("a3", ctypes.c_float), ("a4", ctypes.c_float), ("cg_c", ctypes.c_double),
+    ]
+
+
+GR_SOLVER_LANDWEBER, GR_SOLVER_CG, GR_SOLVER_TV = 0, 1, 2
+GR_BATCH_NORMEST, GR_BATCH_MAIN, GR_BATCH_CG_INIT = 0, 1, 2
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _F = ctypes.c_float
@@ -65,10 +87,16 @@ SIGNATURES = {
     "gr_backward_sum": (_I, [_G, _P, _P, _P, _I, _I, _P]),
     "gr_forward_wsq_noalloc": (_I, [_G, _P, _P, _P, _P, _I, _I, _P]),
     "gr_forward_angle_axpy": (_I, [_G, _P, _P, _P, _P, _D, _I, _I, _P]),
-    "gr_backward_tv_adjoint": (_I, [_G, _P, _P, _P, _F, _F, _F, _I, _I, _P]),
+    "gr_backward_tv_adjoint": (_I, [_G, _P, _P, _P, _D, _F, _F, _I, _I, _P]),
     "gr_tv_adjoint_primal": (_I, [_P, _P, _P, _P, _P, _I, _Z, _P]),
     "gr_tv_adjoint_dual": (_I, [_P, _P, _P, _P, _P, _F, _F, _F, _I, _I, _I, _I, _I, _P]),
     "gr_tv_adjoint_lambda": (_I, [_P, _P, _P, _F, _F, _I, _Z, _P]),
+    "gr_batch_problem_size": (_Z, []),
+    "gr_batch_forward": (_I, [_P, _P, _I, _I, _I, _P]),
+    "gr_batch_backward": (_I, [_P, _P, _I, _I, _I, _P]),
+    "gr_batch_image_step": (_I, [_P, _P, _I, _I, _I, _P]),
+    "gr_batch_sino_step": (_I, [_P, _P, _I, _I, _I, _P]),
+    "gr_batch_scalars": (_I, [_P, _P, _I, _I, _I, _P]),
     "gr_forward_partials": (_Z, [_G, _I]),
     "gr_backward_partials": (_Z, [_G, _I, _I]),
     "gr_weight_sinogram": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),

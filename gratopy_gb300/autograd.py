@@ -183,10 +183,10 @@ class _TVProblem:
         c3 = -float(self.tau) * float(self.norming) / self.ps.forward_scale(self.ndt)
         _lib.call("gr_forward_angle_axpy", ctypes.byref(self.g), _ptr(tmp.L), _ptr(adj.L), _ptr(gz),
                   _ptr(self.w), c3, self.Nz, self.of, st)
-        # Lambda' = mu2 (Lambda + sigma_l (A Ubar - f))
+        # Lambda' = mu2 (Lambda + sigma_l (A Ubar - f)); the kernels apply the
+        # two float32 factors one after the other, so the product stays unrounded
         _lib.call("gr_backward_tv_adjoint", ctypes.byref(self.ga), _ptr(adj.Ubar), _ptr(tmp.L),
-                  _ptr(tmp.V), float(np.float32(self.mu2 * self.sigma_l)), self.sigma, self.z,
-                  self.Nz, self.of, st)
+                  _ptr(tmp.V), self.mu2 * self.sigma_l, self.sigma, self.z, self.Nz, self.of, st)
         _lib.call("gr_tv_adjoint_lambda", _ptr(adj.L), _ptr(gf), _ptr(tmp.L), self.mu2,
                   self.sigma_l, _dt(self.f), adj.L.numel(), st)
         adj.U.copy_(gu_prev)

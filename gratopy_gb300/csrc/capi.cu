@@ -143,7 +143,7 @@ int gr_forward_angle_axpy(const gr_geometry* g, void* out, const void* base, con
 }
 
 int gr_backward_tv_adjoint(const gr_geometry* g, void* out, const void* lambda, const void* gw,
-                           float c1, float sigma, float z_distance, int Nz, int order,
+                           double c1, float sigma, float z_distance, int Nz, int order,
                            void* stream) {
   if (!same_order_ok(g, order) || out == nullptr || lambda == nullptr || gw == nullptr)
     return GR_ERR_ARG;

@@ -79,6 +79,11 @@ __device__ __forceinline__ double gmax(double a, double b) { return fmax(a, b); 
 __device__ __forceinline__ float ghypot(float a, float b) { return hypotf(a, b); }
 __device__ __forceinline__ double ghypot(double a, double b) { return hypot(a, b); }
 
+// Linear index of the current block in its grid.
+__device__ __forceinline__ int64_t bid_linear() {
+  return blockIdx.x + (int64_t)gridDim.x * ((int64_t)blockIdx.y + (int64_t)gridDim.y * blockIdx.z);
+}
+
 // Deterministic block-wide sum of one double per thread.  Every thread of the
 // block must call it; the result is valid in thread 0.  `red` must hold one
 // double per warp.

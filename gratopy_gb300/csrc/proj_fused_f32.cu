@@ -16,6 +16,6 @@ template int bwd_cg<float>(const gr_geometry*, void*, const void*, void*, const 
 template int bwd_sum<float>(const gr_geometry*, void*, const void*, double*, int, int, void*);
 template int fwd_angle_axpy<float>(const gr_geometry*, void*, const void*, const void*, const void*,
                                 double, int, int, void*);
-template int bwd_tv_adjoint<float>(const gr_geometry*, void*, const void*, const void*, float, float,
+template int bwd_tv_adjoint<float>(const gr_geometry*, void*, const void*, const void*, double, float,
                                 float, int, int, void*);
 }  // namespace gr

@@ -16,6 +16,6 @@ template int bwd_cg<double>(const gr_geometry*, void*, const void*, void*, const
 template int bwd_sum<double>(const gr_geometry*, void*, const void*, double*, int, int, void*);
 template int fwd_angle_axpy<double>(const gr_geometry*, void*, const void*, const void*, const void*,
                                 double, int, int, void*);
-template int bwd_tv_adjoint<double>(const gr_geometry*, void*, const void*, const void*, float, float,
+template int bwd_tv_adjoint<double>(const gr_geometry*, void*, const void*, const void*, double, float,
                                 float, int, int, void*);
 }  // namespace gr

@@ -42,7 +42,7 @@ template <typename T>
 int fwd_angle_axpy(const gr_geometry* g, void* out, const void* base, const void* u,
                    const void* w, double c, int Nz, int order, void* stream);
 template <typename T>
-int bwd_tv_adjoint(const gr_geometry* g, void* out, const void* lambda, const void* gw, float c1,
+int bwd_tv_adjoint(const gr_geometry* g, void* out, const void* lambda, const void* gw, double c1,
                    float sigma, float z_distance, int Nz, int order, void* stream);
 
 #ifdef GR_DEFINE_PLAIN
@@ -165,12 +165,12 @@ int fwd_angle_axpy(const gr_geometry* g, void* out, const void* base, const void
 }
 
 template <typename T>
-int bwd_tv_adjoint(const gr_geometry* g, void* out, const void* lambda, const void* gw, float c1,
+int bwd_tv_adjoint(const gr_geometry* g, void* out, const void* lambda, const void* gw, double c1,
                    float sigma, float z_distance, int Nz, int order, void* stream) {
   const Dims d = launch::dims_of(g, Nz);
   return dispatch_order(order, [&](auto o) {
     constexpr int O = decltype(o)::value;
-    BwdTVAdjoint<T, O> e{static_cast<T*>(out), static_cast<const T*>(gw), d, c1, sigma,
+    BwdTVAdjoint<T, O> e{static_cast<T*>(out), static_cast<const T*>(gw), d, (T)c1, sigma,
                          z_distance};
     return launch::launch_bwd<T, O, O>(g, lambda, Nz, e, nullptr, nullptr, stream);
   });

@@ -197,7 +197,8 @@ struct BwdTVAdjoint {
   T* out;
   const T* gw;
   Dims d;
-  float c1, sigma, z_distance;
+  T c1;
+  float sigma, z_distance;
   __device__ __forceinline__ double operator()(int64_t x, int64_t y, int64_t z, int64_t i,
                                                T v) const {
     int64_t sx, sy, sz;

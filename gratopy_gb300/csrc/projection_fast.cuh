@@ -91,21 +91,18 @@ __device__ __forceinline__ void stage_windows(Window<ZB>& win, const Rec* rec, i
 }
 
 template <int IO, int SO, int ZB, int ASPLIT, int PY, class Epi>
-__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
-radon_bwd_fast(const float* __restrict__ sino, const float* __restrict__ ofs, Dims d, Epi epi,
-               double* __restrict__ partials, const int* __restrict__ skip) {
+__device__ __forceinline__ double radon_bwd_fast_tile(const float* __restrict__ sino, const float* __restrict__ ofs, Dims d, Epi epi,
+               uint3 bid) {
   using TL = Tile<ASPLIT, PY>;
   constexpr int kWinAngles = WinAngles<ZB>::value;
   __shared__ RadonRec rec[kWinAngles];
   __shared__ Window<ZB> win;
-  __shared__ double red[kBwdTileFast * kBwdTileSlow / 32];
-  if (skip != nullptr && *skip) return;
   const int g = threadIdx.y % ASPLIT;
-  const int64_t f0 = (int64_t)blockIdx.x * kBwdTileFast;
-  const int64_t s0 = (int64_t)blockIdx.y * TL::kSlow;
+  const int64_t f0 = (int64_t)bid.x * kBwdTileFast;
+  const int64_t s0 = (int64_t)bid.y * TL::kSlow;
   const int64_t fast = f0 + threadIdx.x;
   const int64_t slow0 = s0 + threadIdx.y / ASPLIT;
-  const int64_t z0 = (int64_t)blockIdx.z * ZB;
+  const int64_t z0 = (int64_t)bid.z * ZB;
   const int zn = (int)min((int64_t)ZB, d.Nz - z0);
   // tile corners in (x, y)
   const float fx0 = (float)(IO == ORDER_F ? f0 : s0);
@@ -233,30 +230,37 @@ radon_bwd_fast(const float* __restrict__ sino, const float* __restrict__ ofs, Di
       }
     }
   }
-  if (Epi::kReduce) {
-    double t = block_sum(part, red);
-    if (tid == 0)
-      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
-  }
+  return part;
 }
 
 template <int IO, int SO, int ZB, int ASPLIT, int PY, class Epi>
 __global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
-fan_bwd_fast(const float* __restrict__ sino, const float* __restrict__ ofs,
+radon_bwd_fast(const float* __restrict__ sino, const float* __restrict__ ofs, Dims d, Epi epi,
+               double* __restrict__ partials, const int* __restrict__ skip) {
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const double part = radon_bwd_fast_tile<IO, SO, ZB, ASPLIT, PY, Epi>(sino, ofs, d, epi, blockIdx);
+  if (Epi::kReduce) {
+    double t = block_sum(part, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0)
+      partials[bid_linear()] = t;
+  }
+}
+
+template <int IO, int SO, int ZB, int ASPLIT, int PY, class Epi>
+__device__ __forceinline__ double fan_bwd_fast_tile(const float* __restrict__ sino, const float* __restrict__ ofs,
              const float* __restrict__ sdpd, FanGeo<float> gg, Dims d, Epi epi,
-             double* __restrict__ partials, const int* __restrict__ skip) {
+             uint3 bid) {
   using TL = Tile<ASPLIT, PY>;
   constexpr int kWinAngles = WinAngles<ZB>::value;
   __shared__ FanRec rec[kWinAngles];
   __shared__ Window<ZB> win;
-  __shared__ double red[kBwdTileFast * kBwdTileSlow / 32];
-  if (skip != nullptr && *skip) return;
   const int g = threadIdx.y % ASPLIT;
-  const int64_t f0 = (int64_t)blockIdx.x * kBwdTileFast;
-  const int64_t s0 = (int64_t)blockIdx.y * TL::kSlow;
+  const int64_t f0 = (int64_t)bid.x * kBwdTileFast;
+  const int64_t s0 = (int64_t)bid.y * TL::kSlow;
   const int64_t fast = f0 + threadIdx.x;
   const int64_t slow0 = s0 + threadIdx.y / ASPLIT;
-  const int64_t z0 = (int64_t)blockIdx.z * ZB;
+  const int64_t z0 = (int64_t)bid.z * ZB;
   const int zn = (int)min((int64_t)ZB, d.Nz - z0);
   const float fx0 = (float)(IO == ORDER_F ? f0 : s0) - gg.midx;
   const float fy0 = (float)(IO == ORDER_F ? s0 : f0) - gg.midy;
@@ -409,10 +413,21 @@ fan_bwd_fast(const float* __restrict__ sino, const float* __restrict__ ofs,
       }
     }
   }
+  return part;
+}
+
+template <int IO, int SO, int ZB, int ASPLIT, int PY, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+fan_bwd_fast(const float* __restrict__ sino, const float* __restrict__ ofs,
+             const float* __restrict__ sdpd, FanGeo<float> gg, Dims d, Epi epi,
+             double* __restrict__ partials, const int* __restrict__ skip) {
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const double part = fan_bwd_fast_tile<IO, SO, ZB, ASPLIT, PY, Epi>(sino, ofs, sdpd, gg, d, epi, blockIdx);
   if (Epi::kReduce) {
     double t = block_sum(part, red);
-    if (tid == 0)
-      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0)
+      partials[bid_linear()] = t;
   }
 }
 
@@ -433,9 +448,9 @@ struct GroupLayout {
   static constexpr int kRaysPerBlock = kGroupsPerWarp * kRayGroup * (kFwdBlock / 32);
   int64_t s0;
   int lane_group;
-  __device__ __forceinline__ GroupLayout() {
+  __device__ __forceinline__ explicit GroupLayout(uint3 bid) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    s0 = (int64_t)blockIdx.x * kRaysPerBlock +
+    s0 = (int64_t)bid.x * kRaysPerBlock +
          ((int64_t)warp * kGroupsPerWarp + lane % kGroupsPerWarp) * kRayGroup;
     lane_group = lane / kGroupsPerWarp;
   }
@@ -469,15 +484,12 @@ __device__ __forceinline__ void row_range(float a_lo, float b_lo, float a_hi, fl
 }
 
 template <int SO, int IO, int ZB, int SPLIT, class Epi>
-__global__ void __launch_bounds__(kFwdBlock)
-radon_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs, RadonGeo<float> g,
-               Dims d, Epi epi, double* __restrict__ partials, const int* __restrict__ skip) {
-  __shared__ double red[kFwdBlock / 32];
-  if (skip != nullptr && *skip) return;
-  const GroupLayout<SPLIT> L;
+__device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ img, const float* __restrict__ ofs, RadonGeo<float> g,
+               Dims d, Epi epi, uint3 bid) {
+  const GroupLayout<SPLIT> L(bid);
   const int64_t s0 = L.s0;
-  const int64_t a = blockIdx.y;
-  const int64_t z0 = (int64_t)blockIdx.z * ZB;
+  const int64_t a = bid.y;
+  const int64_t z0 = (int64_t)bid.z * ZB;
   const bool active = s0 < d.Ns;
   const int zn = (int)min((int64_t)ZB, d.Nz - z0);
   float acc[kRayGroup][ZB];
@@ -554,24 +566,31 @@ radon_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs, Rad
       }
     }
   }
-  if (Epi::kReduce) {
-    double t = block_sum(part, red);
-    if (threadIdx.x == 0)
-      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
-  }
+  return part;
 }
 
 template <int SO, int IO, int ZB, int SPLIT, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
-fan_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs,
-             const float* __restrict__ sdpd, FanGeo<float> g, Dims d, Epi epi,
-             double* __restrict__ partials, const int* __restrict__ skip) {
-  __shared__ double red[kFwdBlock / 32];
+radon_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs, RadonGeo<float> g,
+               Dims d, Epi epi, double* __restrict__ partials, const int* __restrict__ skip) {
+  __shared__ double red[32];
   if (skip != nullptr && *skip) return;
-  const GroupLayout<SPLIT> L;
+  const double part = radon_fwd_fast_tile<SO, IO, ZB, SPLIT, Epi>(img, ofs, g, d, epi, blockIdx);
+  if (Epi::kReduce) {
+    double t = block_sum(part, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0)
+      partials[bid_linear()] = t;
+  }
+}
+
+template <int SO, int IO, int ZB, int SPLIT, class Epi>
+__device__ __forceinline__ double fan_fwd_fast_tile(const float* __restrict__ img, const float* __restrict__ ofs,
+             const float* __restrict__ sdpd, FanGeo<float> g, Dims d, Epi epi,
+             uint3 bid) {
+  const GroupLayout<SPLIT> L(bid);
   const int64_t s0 = L.s0;
-  const int64_t a = blockIdx.y;
-  const int64_t z0 = (int64_t)blockIdx.z * ZB;
+  const int64_t a = bid.y;
+  const int64_t z0 = (int64_t)bid.z * ZB;
   const bool active = s0 < d.Ns;
   const int zn = (int)min((int64_t)ZB, d.Nz - z0);
   float acc[kRayGroup][ZB];
@@ -675,10 +694,21 @@ fan_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs,
       }
     }
   }
+  return part;
+}
+
+template <int SO, int IO, int ZB, int SPLIT, class Epi>
+__global__ void __launch_bounds__(kFwdBlock)
+fan_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs,
+             const float* __restrict__ sdpd, FanGeo<float> g, Dims d, Epi epi,
+             double* __restrict__ partials, const int* __restrict__ skip) {
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const double part = fan_fwd_fast_tile<SO, IO, ZB, SPLIT, Epi>(img, ofs, sdpd, g, d, epi, blockIdx);
   if (Epi::kReduce) {
     double t = block_sum(part, red);
-    if (threadIdx.x == 0)
-      partials[blockIdx.x + gridDim.x * ((int64_t)blockIdx.y + gridDim.y * (int64_t)blockIdx.z)] = t;
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0)
+      partials[bid_linear()] = t;
   }
 }
 

@@ -141,7 +141,7 @@ GR_API int gr_forward_angle_axpy(const gr_geometry* g, void* out, const void* ba
  * total_variation.cl:54-167): out = c1 * (A^T lambda) - sigma * div(gw) on
  * the image, with A^T from an adjoint geometry as above. */
 GR_API int gr_backward_tv_adjoint(const gr_geometry* g, void* out, const void* lambda,
-                                  const void* gw, float c1, float sigma, float z_distance, int Nz,
+                                  const void* gw, double c1, float sigma, float z_distance, int Nz,
                                   int order, void* stream);
 /* Elementwise parts of the TV adjoint (csrc/tv_adjoint.cu):
  * gz = [u_next > 0] (gu + 2 gubar), gu_prev = gz - gubar */
@@ -184,6 +184,55 @@ GR_API int gr_sum_values_partials(double* partials, const void* a, int dtype, si
  * v = P_{|.|<=1}(v + sigma grad(ubar)); v holds 4 reals per pixel. */
 GR_API int gr_tv_dual(void* v, const void* ubar, float sigma, float z_distance, int dtype, int Nx,
                int Ny, int Nz, int order, void* stream);
+
+/* ---- Batched reconstruction (no counterpart in the reference) ----
+ * Many float32 2-D problems of different sizes, geometries and solvers
+ * advance together: each phase of an iteration is ONE persistent launch
+ * whose blocks stride over a work list of (problem, tile) pairs covering
+ * every problem.  Descriptors, work lists and buffers are device memory
+ * owned by the caller; Fortran order throughout. */
+enum { GR_SOLVER_LANDWEBER = 0, GR_SOLVER_CG = 1, GR_SOLVER_TV = 2 };
+enum { GR_BATCH_NORMEST = 0, GR_BATCH_MAIN = 1, GR_BATCH_CG_INIT = 2 };
+typedef struct gr_batch_problem {
+  int kind, Nx, Ny, Ns, Na, solver;
+  int fwd_split;               /* 2, 4 or 8 lanes per group of detector bins */
+  int fwd_tiles_x;             /* forward tiles per angle */
+  int bwd_tiles_x, bwd_tiles_y;/* backprojection tiles (32 x 8 pixels) */
+  const float* ofs;            /* 8*Na */
+  const float* sdpd;           /* Ns (fan) */
+  const float* w;              /* angle weights, Na */
+  float geo[8];                /* Radon: dx, dxi (float); fan: R, RE, dxi, midx, midy, mid_det, dx */
+  const float* f;              /* data sinogram */
+  float* img;                  /* iterate: normest image / Landweber u / CG x / TV U */
+  float* s1;                   /* normest sino / Landweber residual / CG q / TV lambda */
+  float* s2;                   /* CG d */
+  float* i1;                   /* CG p / TV ubar */
+  float* i2;                   /* CG snew */
+  float* v4;                   /* TV dual, 4 reals per pixel */
+  double* sc;                  /* GR_SC_COUNT scalars */
+  double* fwd_part;            /* fwd_tiles_x * Na partials */
+  double* bwd_part;            /* bwd_tiles_x * bwd_tiles_y partials */
+  float a0, a1, a2, a3, a4;    /* Landweber: a0 = -w;  TV: sigma, sigma_l, mu2, tau, norming */
+  double cg_c;                 /* CG: dx^2/ds */
+} gr_batch_problem;
+/* sizeof(gr_batch_problem), so bindings can check their struct layout. */
+GR_API size_t gr_batch_problem_size(void);
+/* items: 2*n ints (problem index, tile index); grid: persistent block count. */
+GR_API int gr_batch_forward(const gr_batch_problem* probs, const int* items, int n, int mode,
+                            int grid, void* stream);
+GR_API int gr_batch_backward(const gr_batch_problem* probs, const int* items, int n, int mode,
+                             int grid, void* stream);
+/* image-sized elementwise step over backprojection tiles: normest scaling,
+ * CG p = beta p + snew, TV dual update */
+GR_API int gr_batch_image_step(const gr_batch_problem* probs, const int* items, int n, int mode,
+                               int grid, void* stream);
+/* sinogram-sized elementwise step (CG d -= alpha q) over chunks of 256 bins */
+GR_API int gr_batch_sino_step(const gr_batch_problem* probs, const int* items, int n, int mode,
+                              int grid, void* stream);
+/* per-problem scalar step, one block per listed problem (phase 0: after the
+ * forward launch, phase 1: after the backprojection) */
+GR_API int gr_batch_scalars(const gr_batch_problem* probs, const int* prob_ids, int n, int mode,
+                            int phase, void* stream);
 
 /* ---- Device-resident solver scalars ----
  * sc is a device array of GR_SC_COUNT doubles; see the GR_SC_* slots. */

@@ -62,3 +62,7 @@ def test_host_only_entry_points(library):
     assert lib.gr_forward(ctypes.byref(g), None, None, 1, 0, 0, None) == 1
     assert lib.gr_radon_fwd(None, None, None, None, 0, 1, 1, 1, 0, 0, None) == 1
     assert lib.gr_forward_partials(None, 1) == 0
+    # batched descriptors: binding layout equals the library's
+    assert lib.gr_batch_problem_size() == ctypes.sizeof(_lib.GrBatchProblem)
+    assert lib.gr_batch_forward(None, None, 1, 0, 1, None) == 1
+    assert lib.gr_batch_scalars(None, None, 1, 0, 1, None) == 1

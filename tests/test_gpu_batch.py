@@ -1,0 +1,110 @@
+"""Batched persistent reconstruction against the per-call solvers (GPU).
+
+A heterogeneous batch (Radon and fan beam, different image sizes, angle
+counts and solvers) runs through :class:`gratopy_gb300.batch.BatchedReconstruction`;
+every problem must reproduce what the per-call API gives for it alone:
+
+* the batched ``normest`` equals :func:`gratopy_gb300.normest` with the same
+  start vector (same partial-sum layout and order, so to the last bit);
+* Landweber and TV iterates equal the per-call iterates for the same norm
+  estimate (same tile functions and epilogue arithmetic);
+* CG differs from the per-call form only in how the first <p, p> is reduced,
+  so it is held to a float32 tolerance.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _problems(device):
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import batch as gb
+    from gratopy_gb300.phantom import random_ellipse_image
+
+    specs = [
+        ("radon", (40, 36), 30, "landweber", 7),
+        ("fan", (48, 48), 44, "landweber", 5),
+        ("radon", (64, 64), 50, "cg", 6),
+        ("fan", (40, 40), 36, "cg", 9),
+        ("radon", (33, 47), 25, "tv", 8),
+        ("fan", (56, 56), 60, "tv", 4),
+        ("radon", (24, 24), [(20, 0.0, 2.0)], "tv", 11),
+    ]
+    rng = np.random.default_rng(5)
+    out = []
+    for k, (geom, shape, angles, solver, iters) in enumerate(specs):
+        if geom == "radon":
+            ps = gg.ProjectionSettings(device, gg.RADON, shape, angles)
+        else:
+            ps = gg.ProjectionSettings(device, gg.FANBEAM, shape, angles,
+                                       n_detectors=int(1.5 * shape[0]), detector_width=40.0,
+                                       R=70.0, RE=30.0)
+        img = random_ellipse_image(30 + k, shape[::-1], dtype="float32").T
+        img_d = gg.core.empty(shape, torch.float32, "F", device)
+        img_d.copy_(torch.from_numpy(np.ascontiguousarray(img.T)).T)
+        sino = gg.forwardprojection(img_d, ps)
+        sino += 0.5 * torch.rand(sino.shape, generator=torch.Generator(device).manual_seed(k),
+                                 device=device)
+        pr = gb.Problem(ps, sino, solver, iters, mu=15.0 + k)
+        pr.normest_x0 = rng.standard_normal(shape).astype(np.float32)
+        out.append(pr)
+    return out
+
+
+def test_batched_matches_per_call(cuda_device):
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import batch as gb
+
+    problems = _problems(cuda_device)
+    runner = gb.BatchedReconstruction(problems, cuda_device, normest_iterations=20)
+    results = runner.run()
+    for pr, got in zip(problems, results):
+        ps = pr.settings
+        if pr.solver in ("landweber", "tv"):
+            want_n = gg.normest(ps, 20, x0=pr.normest_x0)
+            assert abs(pr.norm_estimate - want_n) <= 1e-12 * want_n
+        if pr.solver == "landweber":
+            want = gg.landweber(pr.sino, ps, pr.iterations, w=pr.w, norm_estimate=pr.norm_estimate)
+        elif pr.solver == "cg":
+            want = gg.conjugate_gradients(pr.sino, ps, pr.iterations)
+        else:
+            want = gg.total_variation(pr.sino, ps, pr.mu, pr.iterations,
+                                      stepsize_weighting=pr.stepsize_weighting,
+                                      norm_estimate=pr.norm_estimate)
+        err = rel_l2(got.cpu().numpy(), want.cpu().numpy())
+        tol = 1e-5 if pr.solver == "cg" else 1e-6
+        assert err <= tol, f"{pr.solver} {ps.geometry} {ps.img_shape}: rel err {err:.3e}"
+
+
+def test_batched_graph_and_direct_agree(cuda_device):
+    from gratopy_gb300 import batch as gb
+
+    a = gb.BatchedReconstruction(_problems(cuda_device), cuda_device, normest_iterations=10,
+                                 use_graph=True).run()
+    b = gb.BatchedReconstruction(_problems(cuda_device), cuda_device, normest_iterations=10,
+                                 use_graph=False).run()
+    for x, y in zip(a, b):
+        assert (x == y).all()
+
+
+def test_heterogeneous_generator_runs(cuda_device):
+    import torch
+
+    from gratopy_gb300 import batch as gb
+
+    problems = gb.heterogeneous_problems(6, seed=3, device=cuda_device, landweber_iterations=4,
+                                         cg_iterations=3, tv_iterations=5, sizes=(32, 48),
+                                         angle_range=(20, 40))
+    out = gb.BatchedReconstruction(problems, cuda_device, normest_iterations=5).run()
+    assert len(out) == 6
+    for x, pr in zip(out, problems):
+        assert tuple(x.shape) == tuple(pr.settings.img_shape)
+        assert torch.isfinite(x).all()
