@@ -97,7 +97,7 @@ class ClockSampler:
         try:
             self._proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (FileNotFoundError, OSError):
             self._proc = None
@@ -109,6 +109,9 @@ class ClockSampler:
 
         self._thread = threading.Thread(target=reader, daemon=True)
         self._thread.start()
+        t0 = time.time()
+        while not self.rows and time.time() - t0 < 3.0 and self._proc.poll() is None:
+            time.sleep(0.01)
         return self
 
     def stop(self):
@@ -157,6 +160,11 @@ def run_gpu(args, rank, world, device):
     back = gg.core.empty(img_shape, torch.float32, "F", device)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
     stream = torch.cuda.current_stream(device)
+
+    from gratopy_gb300 import autotune
+
+    t = autotune.tune(ps, np.float32, use_cache=False)
+    tuned = {"fwd_split": t["fwd_split"], "bwd_split": t["bwd_split"]}
 
     def step(ev=None):
         if ev is not None:
@@ -223,7 +231,119 @@ def run_gpu(args, rank, world, device):
         raise RuntimeError("end-to-end result differs from the device-resident run")
 
     return dict(total=total, t_fwd=t_fwd, t_bwd=t_bwd, clocks=clocks, e2e_total=e2e_total,
-                h2d=h_img.numel() * 4, d2h=h_back.numel() * 4, ps=ps)
+                h2d=h_img.numel() * 4, d2h=h_back.numel() * 4, ps=ps, tuned=tuned, flush=flush,
+                img=img)
+
+
+def _event_times(fn, reps, flush=None):
+    """Device seconds of ``fn()`` per repetition (CUDA events on the current stream)."""
+    import torch
+
+    out = []
+    for _ in range(reps):
+        if flush is not None:
+            flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        out.append(a.elapsed_time(b) * 1e-3)
+    return out
+
+
+def extra_radon256(device, flush):
+    """Plain Radon forward + backprojection, 256 x 256, 180 angles, 363 detectors."""
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300.phantom import random_ellipse_image
+
+    res = {}
+    host = random_ellipse_image(SEED, (256, 256), count=10, dtype="float64").T
+    for name, tdt in (("float32", torch.float32), ("float64", torch.float64)):
+        ps = gg.ProjectionSettings(device, gg.RADON, (256, 256), 180, n_detectors=363)
+        img = gg.core.empty((256, 256), tdt, "F", device)
+        img.copy_(torch.from_numpy(np.ascontiguousarray(host.T)).T)
+        sino = gg.core.empty(ps.sinogram_shape, tdt, "F", device)
+        back = gg.core.empty((256, 256), tdt, "F", device)
+
+        def step():
+            gg.forwardprojection(img, ps, sino=sino)
+            gg.backprojection(sino, ps, img=back)
+
+        _event_times(step, 3, flush)
+        t = _event_times(step, 50, flush)
+        res[name] = 2 * 256 * 256 * 180 / statistics.median(t) / 1e9
+    return {"workload": "radon 256x256, 180 angles [0,pi), 363 detectors, fwd+back, L2 flushed",
+            "unit": UNIT, **res}
+
+
+def extra_cg50(device, ps, img):
+    """50-iteration CG reconstruction of the headline fan-beam workload (1% noise)."""
+    import torch
+
+    import gratopy_gb300 as gg
+
+    sino = gg.forwardprojection(img, ps)
+    gen = torch.Generator(device=device).manual_seed(SEED)
+    noise = torch.randn(sino.shape, generator=gen, device=device)
+    sino += 0.01 * float(sino.abs().max()) * noise
+    run = lambda: gg.conjugate_gradients(sino, ps, 50)  # noqa: E731
+    _event_times(run, 2)
+    t = _event_times(run, 5)
+    return {"workload": "fanbeam 512x512, 360 angles, 768 detectors, 50 CG iterations, "
+                        "1% Gaussian noise", "recon_per_s": 1.0 / statistics.median(t),
+            "ms_per_recon": statistics.median(t) * 1e3}
+
+
+def extra_batched(device, small=False):
+    """Heterogeneous batch of 64 problems: batched persistent launches against per-call."""
+    import torch
+
+    from gratopy_gb300 import batch as gb
+
+    kw = dict(sizes=(32, 48, 64, 96, 128), angle_range=(30, 180)) if small else {}
+    probs = gb.heterogeneous_problems(64, seed=0, device=device, **kw)
+
+    def fresh():
+        return [gb.Problem(p.settings, p.sino, p.solver, p.iterations, mu=p.mu) for p in probs]
+
+    def wall(fn):
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize(device)
+        return time.perf_counter() - t0, out
+
+    gb.BatchedReconstruction(fresh()[:6], device, normest_iterations=3, autotune=True).run()
+    gb.solve_plain(fresh()[:6])
+    t_b, _ = wall(lambda: gb.BatchedReconstruction(fresh(), device, autotune=True).run())
+    solved = fresh()
+    t_b2, out_b = wall(lambda: gb.BatchedReconstruction(solved, device, autotune=True).run())
+    t_b = min(t_b, t_b2)
+    t_pg, _ = wall(lambda: gb.solve_plain(fresh(), use_graph=True))
+    t_pd, _ = wall(lambda: gb.solve_plain(fresh(), use_graph=False))
+    # accuracy: the per-call solvers with the batch's norm estimates and launch
+    # shapes (batched backprojection tiles use one thread row per angle set)
+    for p in solved:
+        p.settings.gr_geometry(np.float32).bwd_split = 1
+    same = [gb.Problem(p.settings, p.sino, p.solver, p.iterations, mu=p.mu,
+                       norm_estimate=p.norm_estimate) for p in solved]
+    ref = gb.solve_plain(same)
+    err = {}
+    for p, a, b in zip(solved, out_b, ref):
+        e = float(torch.linalg.norm((a - b).double()) / torch.linalg.norm(b.double()))
+        err[p.solver] = max(err.get(p.solver, 0.0), e)
+    name = ("64 problems, side U{32..128}, angles U[30,180]" if small else
+            "64 problems, side U{128,192,256,384,512}, angles U[60,720]")
+    return {"workload": name + ", half Radon (full or 2pi/3 range) half fan beam, "
+                        "Landweber-200 / CG-50 / TV-100, float32, normest included",
+            "batched_recon_per_s": 64 / t_b, "plain_graph_recon_per_s": 64 / t_pg,
+            "plain_direct_recon_per_s": 64 / t_pd, "speedup_vs_plain_direct": t_pd / t_b,
+            "speedup_vs_plain_graph": t_pg / t_b, "max_rel_err_vs_per_call": err,
+            "timing": "wall clock around the whole solve, synchronised"}
 
 
 def cpu_baseline_sample(max_seconds=12.0):
@@ -250,10 +370,12 @@ def cpu_baseline_sample(max_seconds=12.0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gratopy_gb300", choices=["gratopy_gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the secondary workloads (Radon 256, CG-50, batched)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -299,7 +421,7 @@ def main():
     Nx, Ny = ps.img_shape
     compulsory = (Nx * Ny + Ns * Na) * 4
     fwd, bwd = statistics.mean(res["t_fwd"]), statistics.mean(res["t_bwd"])
-    dom, t_dom = ("fan_fwd_kernel", fwd) if fwd >= bwd else ("fan_bwd_kernel", bwd)
+    dom, t_dom = ("fan_fwd_fast", fwd) if fwd >= bwd else ("fan_bwd_fast", bwd)
     achieved = compulsory / t_dom / 1e9
     traffic = None
     tr_file = ROOT / "profiles" / "traffic.json"
@@ -325,6 +447,12 @@ def main():
         "gpu_launches": 2 * steps,
         "clocks": res["clocks"],
     }
+    line["tuned_splits"] = res["tuned"]
+    if not args.no_extras:
+        line["radon256"] = extra_radon256(device, res["flush"])
+        line["cg50"] = extra_cg50(device, ps, res["img"])
+        line["batched"] = extra_batched(device)
+        line["batched_small"] = extra_batched(device, small=True)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
     print(json.dumps(line))

@@ -54,8 +54,15 @@ class BatchedReconstruction:
     """Run a list of :class:`Problem` s together on one GPU."""
 
     def __init__(self, problems, device=None, normest_iterations=50, seed=0, use_graph=True,
-                 graph_chunk=25):
+                 graph_chunk=25, autotune=False):
         self.problems = list(problems)
+        if autotune:
+            # per-geometry forward split from the autotuner; the per-call
+            # projections of the same settings use it too
+            from . import autotune as _at
+
+            for pr in self.problems:
+                pr.fwd_split = _at.tune(pr.settings, np.float32)["fwd_split"]
         self.device = core._device_of(device)
         self.normest_iterations = normest_iterations
         self.use_graph = use_graph
@@ -81,8 +88,8 @@ class BatchedReconstruction:
                 raise ValueError(f"unknown solver {pr.solver!r}")
             if tuple(pr.sino.shape) != tuple(ps.sinogram_shape) or pr.sino.dtype != torch.float32:
                 raise ValueError("batched problems are float32 2-D sinograms of the settings' shape")
-            if pr.fwd_split not in (2, 4, 8):
-                raise ValueError("fwd_split must be 2, 4 or 8")
+            if pr.fwd_split not in (1, 2, 4, 8):
+                raise ValueError("fwd_split must be 1, 2, 4 or 8")
             f = core.empty(ps.sinogram_shape, torch.float32, "F", dev)
             f.copy_(pr.sino)
             Nx, Ny = ps.img_shape

@@ -130,6 +130,7 @@ batch_forward_kernel(const gr_batch_problem* __restrict__ probs, const int2* __r
     const gr_batch_problem& P = probs[item.x];
     double part;
     switch (P.fwd_split) {
+      case 1: part = fwd_item<1>(P, item.y, mode); break;
       case 2: part = fwd_item<2>(P, item.y, mode); break;
       case 4: part = fwd_item<4>(P, item.y, mode); break;
       default: part = fwd_item<8>(P, item.y, mode); break;

@@ -100,11 +100,14 @@ template <typename T>
 __global__ void tv_adj_lambda_kernel(T* __restrict__ gl_prev, T* __restrict__ gf,
                                      const T* __restrict__ gl1, float mu2, float sigma_l,
                                      int64_t n) {
+  // the product of the two float32 factors in the array precision (a float
+  // product would round it)
+  const T c = (T)mu2 * (T)sigma_l;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const T g = gl1[i];
     gl_prev[i] = mu2 * g;
-    gf[i] -= (mu2 * sigma_l) * g;
+    gf[i] -= c * g;
   }
 }
 

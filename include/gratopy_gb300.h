@@ -195,7 +195,7 @@ enum { GR_SOLVER_LANDWEBER = 0, GR_SOLVER_CG = 1, GR_SOLVER_TV = 2 };
 enum { GR_BATCH_NORMEST = 0, GR_BATCH_MAIN = 1, GR_BATCH_CG_INIT = 2 };
 typedef struct gr_batch_problem {
   int kind, Nx, Ny, Ns, Na, solver;
-  int fwd_split;               /* 2, 4 or 8 lanes per group of detector bins */
+  int fwd_split;               /* 1, 2, 4 or 8 lanes per group of detector bins */
   int fwd_tiles_x;             /* forward tiles per angle */
   int bwd_tiles_x, bwd_tiles_y;/* backprojection tiles (32 x 8 pixels) */
   const float* ofs;            /* 8*Na */
