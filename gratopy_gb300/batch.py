@@ -70,10 +70,8 @@ class BatchedReconstruction:
         self.rng = np.random.default_rng(seed)
         if _lib.raw("gr_batch_problem_size")() != ctypes.sizeof(_lib.GrBatchProblem):
             raise RuntimeError("gr_batch_problem layout mismatch between library and binding")
-        sms = torch.cuda.get_device_properties(self.device).multi_processor_count
-        self.grid_fwd = sms * 10
-        self.grid_bwd = sms * 6
-        self.grid_ew = sms * 8
+        # persistent grids: 0 lets the library size one wave of resident blocks
+        self.grid_fwd = self.grid_bwd = self.grid_ew = 0
         self._build()
 
     # ------------------------------------------------------------ setup

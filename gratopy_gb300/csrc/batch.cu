@@ -140,7 +140,9 @@ batch_forward_kernel(const gr_batch_problem* __restrict__ probs, const int2* __r
   }
 }
 
-__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+constexpr int kBatchPY = 2;  // pixels per thread of the batched backprojection
+
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow / kBatchPY)
 batch_backward_kernel(const gr_batch_problem* __restrict__ probs, const int2* __restrict__ items,
                       int n, int mode) {
   __shared__ double red[32];
@@ -155,10 +157,10 @@ batch_backward_kernel(const gr_batch_problem* __restrict__ probs, const int2* __
     const BatchBwdEpi e{&P, mode};
     double part;
     if (P.kind == GR_RADON)
-      part = fast::radon_bwd_fast_tile<ORDER_F, ORDER_F, 1, 1, 1, BatchBwdEpi>(in, P.ofs,
-                                                                              dims2(P), e, bid);
+      part = fast::radon_bwd_fast_tile<ORDER_F, ORDER_F, 1, 1, kBatchPY, BatchBwdEpi>(
+          in, P.ofs, dims2(P), e, bid);
     else
-      part = fast::fan_bwd_fast_tile<ORDER_F, ORDER_F, 1, 1, 1, BatchBwdEpi>(
+      part = fast::fan_bwd_fast_tile<ORDER_F, ORDER_F, 1, 1, kBatchPY, BatchBwdEpi>(
           in, P.ofs, P.sdpd, fan_of(P), dims2(P), e, bid);
     const double t = block_sum(part, red);
     if (threadIdx.x + blockDim.x * threadIdx.y == 0) P.bwd_part[item.y] = t;
@@ -248,12 +250,26 @@ batch_scalar_kernel(const gr_batch_problem* __restrict__ probs, const int* __res
   }
 }
 
+// grid <= 0: one wave of resident blocks (SMs x blocks per SM at the
+// kernel's occupancy), so the blocks stride over the work list in lockstep.
+int resident_grid(void (*k)(const gr_batch_problem*, const int2*, int, int), dim3 block) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+    sms = 152;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, (int)(block.x * block.y * block.z),
+                                                    0) != cudaSuccess || per_sm <= 0)
+    per_sm = 4;
+  return sms * per_sm;
+}
+
 int launch_items(void (*k)(const gr_batch_problem*, const int2*, int, int), dim3 block,
                  const gr_batch_problem* probs, const int* items, int n, int mode, int grid,
                  void* stream) {
-  if (n < 0 || grid <= 0) return GR_ERR_ARG;
+  if (n < 0) return GR_ERR_ARG;
   if (n == 0) return GR_OK;
   if (probs == nullptr || items == nullptr) return GR_ERR_ARG;
+  if (grid <= 0) grid = resident_grid(k, block);
   const int g = grid < n ? grid : n;
   k<<<g, block, 0, as_stream(stream)>>>(probs, reinterpret_cast<const int2*>(items), n, mode);
   return check_launch();
@@ -272,8 +288,8 @@ int gr_batch_forward(const gr_batch_problem* probs, const int* items, int n, int
 
 int gr_batch_backward(const gr_batch_problem* probs, const int* items, int n, int mode, int grid,
                       void* stream) {
-  return launch_items(batch_backward_kernel, dim3(kBwdTileFast, kBwdTileSlow), probs, items, n,
-                      mode, grid, stream);
+  return launch_items(batch_backward_kernel, dim3(kBwdTileFast, kBwdTileSlow / kBatchPY), probs,
+                      items, n, mode, grid, stream);
 }
 
 int gr_batch_image_step(const gr_batch_problem* probs, const int* items, int n, int mode,

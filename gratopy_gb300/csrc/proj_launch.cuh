@@ -111,15 +111,11 @@ inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   return dim3((g->Ns + per_block - 1) / per_block, g->Na, (Nz + ZB - 1) / ZB);
 }
 
-// Pixels per thread along the slow axis of the float32 backprojection tile
-// (2 for single slices, 1 when a thread already carries 4 slices).
-inline int bwd_py(const gr_geometry*, int) { return 1; }
-
 inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
   const int ZB = zblock(Nz);
   const int fast = io == ORDER_F ? g->Nx : g->Ny;
   const int slow = io == ORDER_F ? g->Ny : g->Nx;
-  const int rows = kBwdTileSlow / split * bwd_py(g, Nz);
+  const int rows = kBwdTileSlow / split;  // slow extent of a pixel tile
   return dim3((fast + kBwdTileFast - 1) / kBwdTileFast, (slow + rows - 1) / rows, (Nz + ZB - 1) / ZB);
 }
 
@@ -186,12 +182,15 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
   const dim3 grid = bwd_grid(g, Nz, IO, SPLIT);
   const dim3 block(kBwdTileFast, kBwdTileSlow);
   if constexpr (std::is_same<T, float>::value) {
-    constexpr int PY = 1;
+    // single slices without an angle split: 2 pixels per thread, 128-thread
+    // blocks (a 512^2 image then fits in one wave of resident blocks)
+    constexpr int PY = (SPLIT == 1 && ZB == 1) ? 2 : 1;
+    const dim3 fblock(kBwdTileFast, kBwdTileSlow / PY);
     if (g->kind == GR_RADON) {
-      fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, block, 0, st>>>(
+      fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, fblock, 0, st>>>(
           sino, static_cast<const float*>(g->ofs), d, epi, partials, skip);
     } else {
-      fast::fan_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, block, 0, st>>>(
+      fast::fan_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, fblock, 0, st>>>(
           sino, static_cast<const float*>(g->ofs), static_cast<const float*>(g->sdpd),
           fan_geo<float>(g->geo), d, epi, partials, skip);
     }

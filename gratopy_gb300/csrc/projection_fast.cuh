@@ -36,12 +36,14 @@ __device__ __forceinline__ float rcp_approx(float v) {
 }
 
 // ------------------------------------------------------------ backprojection
-// Block: 32 lanes along the contiguous pixel axis x 8 thread rows; ASPLIT
+// Block: 32 lanes along the contiguous pixel axis x 8/PY thread rows; ASPLIT
 // thread rows share a pixel row and take interleaved angles; each thread owns
-// PY pixels spaced kRows apart along the slow axis.
+// PY pixels spaced kRows apart along the slow axis.  The pixel tile is
+// 32 x 8/ASPLIT whatever PY is.
 template <int ASPLIT, int PY>
 struct Tile {
-  static constexpr int kRows = kBwdTileSlow / ASPLIT;  // pixel rows per thread layer
+  static constexpr int kThreadsY = kBwdTileSlow / PY;  // thread rows of the block
+  static constexpr int kRows = kThreadsY / ASPLIT;     // pixel rows per thread layer
   static constexpr int kSlow = kRows * PY;             // slow extent of the tile
 };
 
@@ -53,8 +55,13 @@ struct RadonRec {
   float4 r;
   int ws, wn;
 };
+// Fan record: with P the pixel centre relative to the image midpoint,
+// t = a.x P.x + a.y P.y + a.z and s = b.x P.x + b.y P.y + b.z (the source
+// offset folded into a.z, b.z); a.w, b.w step t and s between the pixels one
+// thread owns; c = (angle weight / R, detector midpoint - ws).
 struct FanRec {
   float4 a, b;
+  float2 c;
   int ws, wn;
 };
 
@@ -74,7 +81,7 @@ __device__ __forceinline__ void stage_windows(Window<ZB>& win, const Rec* rec, i
   int64_t ss_, sa_, sz_;
   sino_strides<SO>(d, ss_, sa_, sz_);
   const int lane = threadIdx.x, warp = threadIdx.y;
-  for (int j = warp; j < na; j += kBwdTileSlow) {
+  for (int j = warp; j < na; j += (int)blockDim.y) {
     const int w0 = rec[j].ws, wn = rec[j].wn;
     if (w0 == INT_MIN) continue;
     const float* prow = sino + (int64_t)(a0 + j) * sa_ + z0 * sz_;
@@ -157,7 +164,7 @@ __device__ __forceinline__ double radon_bwd_fast_tile(const float* __restrict__ 
           const float s = fmaf(cxs[p], r.x, fmaf(cys[p], r.y, r.z));
           const float fl = floorf(s);
           const float fr = s - fl;
-          const int i = min(max((int)fl, 0), kWin - 2);
+          const unsigned i = min((unsigned)(int)fl, (unsigned)(kWin - 2));
 #pragma unroll
           for (int k = 0; k < ZB; ++k) {
             const float v0 = win.v[j][k][i], v1 = win.v[j][k][i + 1];
@@ -174,7 +181,7 @@ __device__ __forceinline__ double radon_bwd_fast_tile(const float* __restrict__ 
         const float fl = floorf(s);
         const float fr = s - fl;
         if (r.ws != INT_MIN) {
-          const int i = min(max((int)fl, 0), kWin - 2);
+          const unsigned i = min((unsigned)(int)fl, (unsigned)(kWin - 2));
 #pragma unroll
           for (int k = 0; k < ZB; ++k) {
             const float v0 = win.v[j][k][i], v1 = win.v[j][k][i + 1];
@@ -311,8 +318,10 @@ __device__ __forceinline__ double fan_bwd_fast_tile(const float* __restrict__ si
       const int wn = finite ? (int)floorf(hi) + 3 - w0 : kWin + 1;
       const bool fits = finite && wn <= kWin;
       FanRec r;
-      r.a = make_float4(qx, qy, ddx, ddy);
-      r.b = make_float4(dx, dy, o[6] / R, fits ? gg.mid_det - (float)w0 : gg.mid_det);
+      const float rows = (float)TL::kRows;
+      r.a = make_float4(ddx, ddy, -fmaf(ddx, qx, ddy * qy), (IO == ORDER_F ? ddy : ddx) * rows);
+      r.b = make_float4(dx, dy, -fmaf(dx, qx, dy * qy), (IO == ORDER_F ? dy : dx) * rows);
+      r.c = make_float2(o[6] / R, fits ? gg.mid_det - (float)w0 : gg.mid_det);
       r.ws = fits ? w0 : INT_MIN;
       r.wn = fits ? wn : 0;
       rec[tid] = r;
@@ -325,17 +334,23 @@ __device__ __forceinline__ double fan_bwd_fast_tile(const float* __restrict__ si
       for (int jj = 0; jj < kWinAngles / ASPLIT; ++jj) {
         const int j = g + jj * ASPLIT;
         const float4 ra = rec[j].a, rb = rec[j].b;
+        const float2 rc = rec[j].c;
+        float t = fmaf(ra.x, pxs[0], fmaf(ra.y, pys[0], ra.z));
+        float ss = fmaf(rb.x, pxs[0], fmaf(rb.y, pys[0], rb.z));
 #pragma unroll
         for (int p = 0; p < PY; ++p) {
-          const float px = pxs[p] - ra.x, py = pys[p] - ra.y;
-          const float t = fmaf(ra.z, px, ra.w * py);
-          const float ss = fmaf(rb.x, px, rb.y * py);
+          if (p > 0) {
+            t += ra.w;
+            ss += rb.w;
+          }
           const float inv = rcp_approx(t);
-          const float xi = fmaf(ss, inv, rb.w);
-          const float scale = rb.z * inv;
+          const float xi = fmaf(ss, inv, rc.y);
+          const float scale = rc.x * inv;
           const float fl = floorf(xi);
           const float fr = xi - fl;
-          const int i = min(max((int)fl, 0), kWin - 2);
+          // every staged window holds its tile's detector range with a
+          // one-bin margin; the clamp only guards the shared-memory bounds
+          const unsigned i = min((unsigned)(int)fl, (unsigned)(kWin - 2));
 #pragma unroll
           for (int k = 0; k < ZB; ++k) {
             const float v0 = win.v[j][k][i], v1 = win.v[j][k][i + 1];
@@ -346,19 +361,21 @@ __device__ __forceinline__ double fan_bwd_fast_tile(const float* __restrict__ si
     } else {
     for (int j = g; j < na; j += ASPLIT) {
       const FanRec r = rec[j];
+      float t = fmaf(r.a.x, pxs[0], fmaf(r.a.y, pys[0], r.a.z));
+      float ss = fmaf(r.b.x, pxs[0], fmaf(r.b.y, pys[0], r.b.z));
 #pragma unroll
       for (int p = 0; p < PY; ++p) {
-        const float px = pxs[p] - r.a.x;
-        const float py = pys[p] - r.a.y;
-        const float t = fmaf(r.a.z, px, r.a.w * py);
-        const float ss = fmaf(r.b.x, px, r.b.y * py);
+        if (p > 0) {
+          t += r.a.w;
+          ss += r.b.w;
+        }
         const float inv = rcp_approx(t);
-        const float xi = fmaf(ss, inv, r.b.w);
-        const float scale = r.b.z * inv;
+        const float xi = fmaf(ss, inv, r.c.y);
+        const float scale = r.c.x * inv;
         const float fl = floorf(xi);
         const float fr = xi - fl;
         if (r.ws != INT_MIN) {
-          const int i = min(max((int)fl, 0), kWin - 2);
+          const unsigned i = min((unsigned)(int)fl, (unsigned)(kWin - 2));
 #pragma unroll
           for (int k = 0; k < ZB; ++k) {
             const float v0 = win.v[j][k][i], v1 = win.v[j][k][i + 1];

@@ -217,7 +217,8 @@ typedef struct gr_batch_problem {
 } gr_batch_problem;
 /* sizeof(gr_batch_problem), so bindings can check their struct layout. */
 GR_API size_t gr_batch_problem_size(void);
-/* items: 2*n ints (problem index, tile index); grid: persistent block count. */
+/* items: 2*n ints (problem index, tile index); grid: persistent block count,
+ * or <= 0 for one wave of resident blocks at the kernel's occupancy. */
 GR_API int gr_batch_forward(const gr_batch_problem* probs, const int* items, int n, int mode,
                             int grid, void* stream);
 GR_API int gr_batch_backward(const gr_batch_problem* probs, const int* items, int n, int mode,
