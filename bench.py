@@ -346,6 +346,113 @@ def extra_batched(device, small=False):
             "timing": "wall clock around the whole solve, synchronised"}
 
 
+def extra_autograd(device):
+    """Gradient step through Radon projections and an unrolled TV reconstruction.
+
+    16 float32 512 x 512 images (one stack, independent slices), 360 angles in
+    [0, pi), 725 detectors.  loss = ||A x - y||^2 + ||TV_20(A x) - x_true||^2
+    with TV_20 = 20 primal-dual iterations (mu = 20) checkpointed every 5;
+    a step is the forward pass plus ``loss.backward()``.
+    """
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import autograd as ga
+    from gratopy_gb300.phantom import random_ellipse_image
+
+    nz = 16
+    ps = gg.ProjectionSettings(device, gg.RADON, (512, 512), 360, n_detectors=725)
+    truth = np.stack([random_ellipse_image(SEED + k, (512, 512), count=10, dtype="float32").T
+                      for k in range(nz)], -1)
+    x_true = gg.core.empty((512, 512, nz), torch.float32, "F", device)
+    x_true.copy_(torch.from_numpy(np.ascontiguousarray(truth.transpose(2, 1, 0))).permute(2, 1, 0))
+    y = gg.forwardprojection(x_true, ps)
+    gen = torch.Generator(device=device).manual_seed(SEED)
+    y += 0.01 * float(y.abs().max()) * torch.randn(y.shape, generator=gen, device=device)
+    nrm = gg.normest(ps, 50, x0=np.ones(ps.img_shape))
+    x = (0.5 * x_true).detach().requires_grad_(True)
+
+    def step():
+        x.grad = None
+        yh = ga.forward_project(x, ps)
+        u = ga.tv_unrolled(yh, ps, 20.0, number_iterations=20, checkpoint_every=5,
+                           slice_thickness=0.0, norm_estimate=nrm)
+        loss = ((yh - y) ** 2).sum() + ((u - x_true) ** 2).sum()
+        loss.backward()
+
+    _event_times(step, 2)
+    t = statistics.median(_event_times(step, 5))
+    # projections per step: A x, 2 per TV iteration forward, the same again in
+    # the checkpoint replay, 2 per adjoint iteration, A^T for the data term
+    projections = 1 + 2 * 20 + 2 * 20 + 2 * 20 + 1
+    pa = 512 * 512 * 360 * nz
+    return {"workload": "16 x 512^2 Radon stack, 360 angles [0,pi), 725 detectors; "
+                        "||Ax-y||^2 + ||TV20(Ax)-x||^2, checkpoint every 5, forward+backward",
+            "steps_per_s": 1.0 / t, "ms_per_step": t * 1e3, "projections_per_step": projections,
+            "gpixel_angle_per_s": projections * pa / t / 1e9}
+
+
+def extra_large_stack(device, iterations=3, adjoint_iterations=5):
+    """2048 x 2048 x 64 fan-beam stack: TV primal-dual and its adjoint, per iteration.
+
+    1440 angles over [0, 2pi), 2900 detectors, RE = 1000, R = 2000, detector
+    width 2000, automatic image width, mu = 50, slice thickness 1; F order
+    (each slice a plane, 4 slices per thread in the projections).  A full
+    500-iteration reconstruction with a differentiable backward through the
+    last 50 iterations is extrapolated from the measured per-iteration times:
+    500 TV iterations + 50 x (replay + adjoint).
+    """
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import autograd as ga
+    from gratopy_gb300.phantom import random_ellipse_volume
+
+    nz = 64
+    ps = gg.ProjectionSettings(device, gg.FANBEAM, (2048, 2048), 1440, n_detectors=2900,
+                               detector_width=2000.0, R=2000.0, RE=1000.0)
+    vol = random_ellipse_volume(device, (2048, 2048), nz, seed=SEED, order="F")
+    sino = gg.forwardprojection(vol, ps)
+    del vol
+    nrm = gg.normest(ps, 50)
+    tv = lambda k: gg.total_variation(sino, ps, 50.0, k, norm_estimate=nrm)  # noqa: E731
+    tv(1)
+    t_tv = _event_times(lambda: tv(iterations), 1)[0] / iterations
+    f = sino.detach().requires_grad_(True)
+
+    def unrolled():
+        u = ga.tv_unrolled(f, ps, 50.0, number_iterations=adjoint_iterations,
+                           checkpoint_every=adjoint_iterations, slice_thickness=1.0,
+                           norm_estimate=nrm)
+        u.sum().backward()
+
+    t_fb = _event_times(unrolled, 1)[0]
+    # forward pass of the unrolled run = adjoint_iterations TV iterations; the
+    # backward replays them and runs the adjoint iterations
+    t_back_iter = (t_fb - adjoint_iterations * t_tv) / adjoint_iterations
+    pa = 2048 * 2048 * 1440 * nz
+    del f, sino
+    torch.cuda.empty_cache()
+    return {"workload": "fanbeam 2048^2 x 64 slices float32 F order, 1440 angles, 2900 detectors, "
+                        "RE=1000, R=2000; TV mu=50, slice thickness 1",
+            "tv_ms_per_iteration": t_tv * 1e3,
+            "tv_gpixel_angle_per_s": 2 * pa / t_tv / 1e9,
+            "backward_ms_per_iteration": t_back_iter * 1e3,
+            "extrapolated_500_tv_plus_50_backward_s": 500 * t_tv + 50 * t_back_iter,
+            "measured": f"{iterations} TV iterations; {adjoint_iterations} unrolled iterations "
+                        "forward + backward"}
+
+
+EXTRAS = {
+    "radon256": lambda device, ps, res: extra_radon256(device, res["flush"]),
+    "cg50": lambda device, ps, res: extra_cg50(device, ps, res["img"]),
+    "batched": lambda device, ps, res: extra_batched(device),
+    "batched_small": lambda device, ps, res: extra_batched(device, small=True),
+    "autograd": lambda device, ps, res: extra_autograd(device),
+    "large_stack": lambda device, ps, res: extra_large_stack(device),
+}
+
+
 def cpu_baseline_sample(max_seconds=12.0):
     """Time the oracle (restated reference kernels) on this host's cores."""
     from oracle import oracle as O
@@ -375,7 +482,9 @@ def main():
     ap.add_argument("--impl", default="gratopy_gb300", choices=["gratopy_gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the secondary workloads (Radon 256, CG-50, batched)")
+                    help="skip the secondary workloads")
+    ap.add_argument("--extras", default="all",
+                    help="comma list of secondary workloads: " + ",".join(EXTRAS) + " (or all)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -448,11 +557,12 @@ def main():
         "clocks": res["clocks"],
     }
     line["tuned_splits"] = res["tuned"]
-    if not args.no_extras:
-        line["radon256"] = extra_radon256(device, res["flush"])
-        line["cg50"] = extra_cg50(device, ps, res["img"])
-        line["batched"] = extra_batched(device)
-        line["batched_small"] = extra_batched(device, small=True)
+    wanted = [] if args.no_extras else (
+        list(EXTRAS) if args.extras == "all" else [e for e in args.extras.split(",") if e])
+    for name in wanted:
+        if name not in EXTRAS:
+            raise SystemExit(f"unknown extra workload {name!r}; choose from {', '.join(EXTRAS)}")
+        line[name] = EXTRAS[name](device, ps, res)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
     print(json.dumps(line))

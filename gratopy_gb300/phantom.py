@@ -134,3 +134,36 @@ def random_ellipse_image(seed: int, N, count: int = 10, dtype="float32") -> np.n
         M, N = N
     rng = np.random.default_rng(seed)
     return rasterize_ellipses(M, N, random_ellipses(rng, count)).astype(dtype)
+
+
+def ellipse_records(E: np.ndarray) -> np.ndarray:
+    """Per-ellipse records (grey, a^2, b^2, xc, yc, cos theta, sin theta) as the
+    device rasteriser reads them, with the host rasteriser's rounding."""
+    E = np.asarray(E, dtype=np.float64)
+    return np.stack([E[:, 0], E[:, 1] ** 2, E[:, 2] ** 2, E[:, 3], E[:, 4], np.cos(E[:, 5]),
+                     np.sin(E[:, 5])], axis=1)
+
+
+def random_ellipse_volume(device, img_shape, nz: int = 1, seed: int = 0, count: int = 10,
+                          dtype="float32", order: str = "F"):
+    """(Nx, Ny[, nz]) stack rasterised on the device; slice k equals
+    ``random_ellipse_image(seed + k, (Ny, Nx), count, dtype).T``."""
+    import ctypes
+
+    import torch
+
+    from . import _lib, core
+
+    Nx, Ny = (int(img_shape), int(img_shape)) if np.isscalar(img_shape) else map(int, img_shape)
+    recs = np.concatenate([ellipse_records(random_ellipses(np.random.default_rng(seed + k), count))
+                           for k in range(nz)])
+    dev = _device_of(device)
+    tdt = torch.float32 if np.dtype(dtype) == np.float32 else torch.float64
+    shape = (Nx, Ny) + ((nz,) if nz > 1 else ())
+    out = core.empty(shape, tdt, order, dev)
+    e = torch.from_numpy(np.ascontiguousarray(recs.reshape(-1))).to(dev)
+    with torch.cuda.device(dev):
+        _lib.call("gr_ellipses", ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(e.data_ptr()),
+                  count, Nx, Ny, nz, _lib.GR_F32 if tdt == torch.float32 else _lib.GR_F64,
+                  _lib.GR_ORDER_F if order == "F" else _lib.GR_ORDER_C, core._stream_ptr(dev))
+    return out

@@ -185,6 +185,14 @@ GR_API int gr_sum_values_partials(double* partials, const void* a, int dtype, si
 GR_API int gr_tv_dual(void* v, const void* ubar, float sigma, float z_distance, int dtype, int Nx,
                int Ny, int Nz, int order, void* stream);
 
+/* ---- Ellipse phantoms on the device (gratopy phantom.py:159-177) ----
+ * img: Nx x Ny x Nz in `order`; slice z is the sum of its K ellipses, given as
+ * 7 doubles each (grey, a^2, b^2, xc, yc, cos theta, sin theta) at
+ * ellipses[7*K*z ...], on the grid x = linspace(-1,1,Nx), y = -linspace(-1,1,Ny).
+ * Rounded float64 arithmetic in numpy's order: equal to the host rasteriser. */
+GR_API int gr_ellipses(void* img, const double* ellipses, int K, int Nx, int Ny, int Nz, int dtype,
+                       int order, void* stream);
+
 /* ---- Batched reconstruction (no counterpart in the reference) ----
  * Many float32 2-D problems of different sizes, geometries and solvers
  * advance together: each phase of an iteration is ONE persistent launch
