@@ -477,7 +477,7 @@ def cpu_baseline_sample(max_seconds=12.0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gratopy_gb300", choices=["gratopy_gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -351,3 +351,34 @@ def solve_plain(problems, use_graph=False):
                                             stepsize_weighting=pr.stepsize_weighting,
                                             norm_estimate=pr.norm_estimate, use_graph=use_graph))
     return out
+
+
+def _main(argv=None):
+    """Run one seeded heterogeneous batch and print its wall time (``python -m gratopy_gb300.batch``)."""
+    import argparse
+    import json
+    import time
+
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--count", type=int, default=64)
+    ap.add_argument("--small", action="store_true", help="sides 32..128, 30..180 angles")
+    ap.add_argument("--runs", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=0)
+    args = ap.parse_args(argv)
+    dev = core._device_of(None)
+    kw = dict(sizes=(32, 48, 64, 96, 128), angle_range=(30, 180)) if args.small else {}
+    probs = heterogeneous_problems(args.count, seed=args.seed, device=dev, **kw)
+    times = []
+    for _ in range(args.runs):
+        fresh = [Problem(p.settings, p.sino, p.solver, p.iterations, mu=p.mu) for p in probs]
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        BatchedReconstruction(fresh, dev).run()
+        torch.cuda.synchronize(dev)
+        times.append(time.perf_counter() - t0)
+    print(json.dumps({"problems": args.count, "small": args.small, "seconds": times,
+                      "recon_per_s": args.count / min(times)}))
+
+
+if __name__ == "__main__":
+    _main()

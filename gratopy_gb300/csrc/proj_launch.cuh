@@ -92,13 +92,19 @@ inline int fwd_split(const gr_geometry* g, int Nz) {
 
 inline int bwd_split(const gr_geometry* g, int Nz) {
   if (valid_split(g->bwd_split)) return clamp_split(g, g->bwd_split);
-  // float32 backprojection stages detector windows per block; splitting
-  // angles over thread rows multiplies that cost and never paid off.
-  if (g->dtype == GR_F32) return 1;
+  if (g->dtype == GR_F32) {
+    // float32 tiles stage detector windows per block, so angles are split
+    // over thread rows only when the image alone cannot fill 40% of the
+    // GPU's thread slots (single slices: 2 pixels per thread without a split)
+    const int64_t pix = (int64_t)g->Nx * g->Ny * ((Nz + zblock(Nz) - 1) / zblock(Nz));
+    const int64_t want = device_capacity() * 2 / 5;
+    if ((Nz == 1 ? pix / 2 : pix) >= want) return 1;
+    for (int sp = 2; sp < 8; sp <<= 1)
+      if (pix * sp >= want) return sp;
+    return 8;
+  }
   const int64_t work = (int64_t)g->Nx * g->Ny * ((Nz + zblock(Nz) - 1) / zblock(Nz));
-  // float32 tiles stage detector windows per block: splitting angles over
-  // more thread rows multiplies that cost, so one wave is enough there.
-  const int64_t want = (g->dtype == GR_F32 ? 1 : 2) * device_capacity();
+  const int64_t want = 2 * device_capacity();
   for (int sp = 1; sp < 8; sp <<= 1)
     if (work * sp >= want) return clamp_split(g, sp);
   return clamp_split(g, 8);
