@@ -532,13 +532,17 @@ def main():
     fwd, bwd = statistics.mean(res["t_fwd"]), statistics.mean(res["t_bwd"])
     dom, t_dom = ("fan_fwd_fast", fwd) if fwd >= bwd else ("fan_bwd_fast", bwd)
     achieved = compulsory / t_dom / 1e9
-    traffic = None
-    tr_file = ROOT / "profiles" / "traffic.json"
-    if tr_file.exists():
+    # DRAM traffic and issue utilisation of the dominant kernel from the
+    # committed ncu summary of this workload (not measured in this run)
+    traffic, issue = None, None
+    km_file = ROOT / "profiles" / "kernel_metrics.json"
+    if km_file.exists():
         try:
-            traffic = json.loads(tr_file.read_text()).get(dom)
-        except Exception:
-            traffic = None
+            km = json.loads(km_file.read_text()).get(dom, {})
+            traffic = km.get("dram_bytes_per_launch")
+            issue = km.get("issue_active_pct")
+        except (OSError, ValueError):
+            pass
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": res["total"] / steps * 1e3,
@@ -550,7 +554,9 @@ def main():
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
                      "algorithmic_bytes": compulsory, "peak_source": hbm_kind,
-                     "gather_bytes_per_s": 8 * pixel_angles() / t_dom / 1e9},
+                     "gather_bytes_per_s": 8 * pixel_angles() / t_dom / 1e9,
+                     "issue_active_pct_ncu": issue,
+                     "note": "issue-bound gather: compulsory HBM bytes are 2.15 MB per launch"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"]},
         "gpu_launches": 2 * steps,
