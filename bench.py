@@ -235,6 +235,30 @@ def run_gpu(args, rank, world, device):
                 img=img)
 
 
+def l1_load_peak(device, reps=5):
+    """Measured L1 load bandwidth (GB/s, whole GPU): the denominator of the
+    gather roofline.  float4 loads over a 16 KB buffer resident in every SM's
+    L1, one wave of 8 blocks of 256 threads per SM; best of ``reps``."""
+    import ctypes
+
+    import torch
+
+    from gratopy_gb300 import _lib, core
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    n_vec, iters, blocks = 1024, 4096, sms * 8
+    buf = torch.zeros(4 * n_vec, dtype=torch.float32, device=device)
+    out = torch.zeros(blocks * 256, dtype=torch.float32, device=device)
+
+    def run():
+        _lib.call("gr_probe_l1_bandwidth", ctypes.c_void_p(out.data_ptr()),
+                  ctypes.c_void_p(buf.data_ptr()), n_vec, iters, blocks, core._stream_ptr(device))
+
+    run()
+    t = min(_event_times(run, reps))
+    return blocks * 256 * iters * 16 / t / 1e9
+
+
 def _event_times(fn, reps, flush=None):
     """Device seconds of ``fn()`` per repetition (CUDA events on the current stream)."""
     import torch
@@ -563,6 +587,12 @@ def main():
         "clocks": res["clocks"],
     }
     line["tuned_splits"] = res["tuned"]
+    # gather roofline: 8 B per pixel-angle against the measured L1 load rate
+    l1 = l1_load_peak(device)
+    gather = line["roofline"]["gather_bytes_per_s"]
+    line["roofline"]["l1"] = {"gather_gbs": gather, "peak_gbs": l1, "frac": gather / l1,
+                              "peak_source": "measured: gr_probe_l1_bandwidth (float4 loads, "
+                                             "L1-resident buffer)"}
     wanted = [] if args.no_extras else (
         list(EXTRAS) if args.extras == "all" else [e for e in args.extras.split(",") if e])
     for name in wanted:

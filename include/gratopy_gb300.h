@@ -185,6 +185,14 @@ GR_API int gr_sum_values_partials(double* partials, const void* a, int dtype, si
 GR_API int gr_tv_dual(void* v, const void* ubar, float sigma, float z_distance, int dtype, int Nx,
                int Ny, int Nz, int order, void* stream);
 
+/* ---- Measurement (no counterpart in the reference) ----
+ * L1 load-bandwidth probe: `blocks` blocks of 256 threads each stream `iters`
+ * float4 loads from buf (n_vec float4, a power of two, small enough to stay
+ * in L1); bytes moved = blocks * 256 * iters * 16.  out: blocks*256 floats,
+ * written only in a case that cannot occur for a zero buffer. */
+GR_API int gr_probe_l1_bandwidth(float* out, const void* buf, int n_vec, int iters, int blocks,
+                                 void* stream);
+
 /* ---- Ellipse phantoms on the device (gratopy phantom.py:159-177) ----
  * img: Nx x Ny x Nz in `order`; slice z is the sum of its K ellipses, given as
  * 7 doubles each (grey, a^2, b^2, xc, yc, cos theta, sin theta) at
