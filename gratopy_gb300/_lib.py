@@ -93,6 +93,7 @@ SIGNATURES = {
     "gr_tv_adjoint_lambda": (_I, [_P, _P, _P, _F, _F, _I, _Z, _P]),
     "gr_ellipses": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "gr_probe_l1_bandwidth": (_I, [_P, _P, _I, _I, _I, _P]),
+    "gr_sparse_entries": (_I, [_G, _P, _P, _P, _I, _P]),
     "gr_batch_problem_size": (_Z, []),
     "gr_batch_forward": (_I, [_P, _P, _I, _I, _I, _P]),
     "gr_batch_backward": (_I, [_P, _P, _I, _I, _I, _P]),

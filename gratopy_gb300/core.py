@@ -397,42 +397,32 @@ class ProjectionSettings:
     def create_sparse_matrix(self, dtype=np.dtype("float32"), order="F"):
         """Sparse COO matrix of the forward projection (gratopy.py:2014-2155).
 
-        Built column by column from forward projections of unit images on the
-        device; entries <= 0 are dropped as in the reference.
+        One device launch evaluates gratopy's single-line formula
+        (radon.cl:263-341, fanbeam.cl:422-568) for the two detector bins
+        around every pixel's projection; entries that are not positive are
+        dropped as in the reference.  Rows index the sinogram, columns the
+        image, both in the linear order ``order``.
         """
         import scipy.sparse
 
         dtype = _np_dtype(dtype)
         tdt = _torch_dtype(dtype)
-        Nx, Ny = self.img_shape
-        Ns, Na = self.sinogram_shape
         order = order.upper()
         if order not in ("C", "F"):
             raise ValueError("Order (contiguity) not recognized, suitable choices are 'F' or 'C'")
-        n_pix = Nx * Ny
-        batch = max(1, min(n_pix, (1 << 27) // max(1, Ns * Na)))
-        rows, cols, vals = [], [], []
+        Nx, Ny = self.img_shape
+        Ns, Na = self.sinogram_shape
         dev = self.device
-        for start in range(0, n_pix, batch):
-            stop = min(n_pix, start + batch)
-            nb = stop - start
-            img = zeros((Nx, Ny, nb), tdt, "F", dev)
-            flat = torch.arange(start, stop, device=dev)
-            xs = flat % Nx if order == "F" else flat // Ny
-            ys = flat // Nx if order == "F" else flat % Ny
-            img[xs, ys, torch.arange(nb, device=dev)] = 1
-            sino = forwardprojection(img, self)
-            host = sino.cpu().numpy()
-            for k in range(nb):
-                col = start + k
-                s_idx, a_idx = np.nonzero(host[:, :, k] > 0)
-                pos2 = s_idx + Ns * a_idx if order == "F" else s_idx * Na + a_idx
-                rows.append(pos2)
-                cols.append(np.full(len(pos2), col))
-                vals.append(host[s_idx, a_idx, k])
-        rows = np.concatenate(rows) if rows else np.zeros(0, int)
-        cols = np.concatenate(cols) if cols else np.zeros(0, int)
-        vals = np.concatenate(vals) if vals else np.zeros(0, dtype)
+        g = self.gr_geometry(dtype)
+        n = 2 * Nx * Ny * Na
+        rows = torch.empty(n, dtype=torch.int64, device=dev)
+        cols = torch.empty(n, dtype=torch.int64, device=dev)
+        vals = torch.empty(n, dtype=tdt, device=dev)
+        with torch.cuda.device(dev):
+            _lib.call("gr_sparse_entries", ctypes.byref(g), _ptr(rows), _ptr(cols), _ptr(vals),
+                      _oflag(order), _stream_ptr(dev))
+        keep = vals > 0
+        rows, cols, vals = rows[keep].cpu().numpy(), cols[keep].cpu().numpy(), vals[keep].cpu().numpy()
         return scipy.sparse.coo_matrix((vals, (rows, cols)), shape=(Ns * Na, Nx * Ny))
 
     def show_geometry(self, *args, **kwargs):

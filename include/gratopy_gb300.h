@@ -185,6 +185,15 @@ GR_API int gr_sum_values_partials(double* partials, const void* a, int dtype, si
 GR_API int gr_tv_dual(void* v, const void* ubar, float sigma, float z_distance, int dtype, int Nx,
                int Ny, int Nz, int order, void* stream);
 
+/* ---- Sparse matrix of the forward projection (gratopy.py:2014-2155) ----
+ * One launch over (pixel, angle): the single-line formula of radon.cl:263-341
+ * / fanbeam.cl:422-568 for the two bins around the pixel's projection.
+ * rows, cols, vals: 2*Nx*Ny*Na slots each (vals of g's dtype); slot 2*i+c,
+ * i = a + Na*(x + Nx*y), holds (sinogram position, pixel position, value) in
+ * `order`'s linear indexing; value 0 marks a slot without an entry. */
+GR_API int gr_sparse_entries(const gr_geometry* g, int64_t* rows, int64_t* cols, void* vals,
+                             int order, void* stream);
+
 /* ---- Measurement (no counterpart in the reference) ----
  * L1 load-bandwidth probe: `blocks` blocks of 256 threads each stream `iters`
  * float4 loads from buf (n_vec float4, a power of two, small enough to stay
