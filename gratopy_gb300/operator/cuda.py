@@ -22,13 +22,13 @@ class _CUDAOperator(Operator):
     """Shared helpers of operators whose application is a CUDA kernel."""
 
     def __init__(self, *, name=None, kernel_spec=None, **operator_kwargs):
+        from .kernels import CUDAKernelSpec
+
         super().__init__(name=name, **operator_kwargs)
-        if kernel_spec is not None:
-            raise NotImplementedError(
-                "custom OpenCL kernel bundles are not supported by the CUDA build; "
-                "the operator always uses its compiled sm_103a kernels"
-            )
-        self.kernel_spec = None
+        if kernel_spec is not None and not isinstance(kernel_spec, CUDAKernelSpec):
+            raise TypeError("kernel_spec must be a CUDAKernelSpec (CUDA sources or a shared "
+                            "library exporting <base_name>_forward/_backward)")
+        self.kernel_spec = kernel_spec
         self._last_queue = None
 
     def __getstate__(self):

@@ -81,9 +81,35 @@ class _ProjectionOperator(_CUDAOperator):
     def _invoke(self, output, argument, queue):
         ps = self._settings_for(queue)
         self.projection_settings = ps
+        if self.kernel_spec is not None:
+            return self._invoke_custom(ps, output, argument)
         if self.adjoint:
             return ps.backprojection(output, argument, ps)
         return ps.forwardprojection(output, argument, ps)
+
+    def _invoke_custom(self, ps, output, argument):
+        """Run the operator's custom kernel bundle with the gr_forward/gr_backward ABI."""
+        import ctypes
+
+        import torch
+
+        from .. import _lib
+
+        if self.adjoint:
+            core.check_compatibility(output, argument, ps)
+        else:
+            core.check_compatibility(argument, output, ps)
+        forward, backward = self.kernel_spec.functions()
+        fn = backward if self.adjoint else forward
+        g = ps.gr_geometry(core._np_dtype(argument.dtype))
+        dev = argument.device
+        with torch.cuda.device(dev):
+            rc = fn(ctypes.byref(g), output.data_ptr(), argument.data_ptr(), core._nz(argument),
+                    core._oflag(core.order_of(output)), core._oflag(core.order_of(argument)),
+                    core._stream_ptr(dev))
+        if rc != _lib.GR_OK:
+            raise RuntimeError(f"kernel bundle {self.kernel_spec.base_name!r} returned {rc}")
+        return core._event(dev)
 
 
 class Radon(_ProjectionOperator):
