@@ -16,6 +16,9 @@ enum { ORDER_F = 0, ORDER_C = 1 };
 
 struct Dims {
   int64_t Nx, Ny, Nz, Ns, Na;
+  // the array a kernel gathers from is C-ordered with whole groups of 4
+  // slices at 16-byte aligned addresses: 4 slices load as one float4
+  bool vec4 = false;
 };
 
 template <int O>

@@ -53,6 +53,13 @@ inline FanGeo<T> fan_geo(const double* geo) {
 
 inline int zblock(int Nz) { return Nz == 1 ? 1 : 4; }
 
+// C-ordered stacks whose slice count is a multiple of 4 on a 16-byte aligned
+// base keep every 4-slice group of a pixel in one aligned 16-byte word.
+template <typename T>
+inline bool aligned_groups_of_4(const T* base, int Nz) {
+  return Nz % 4 == 0 && (reinterpret_cast<uintptr_t>(base) & 15u) == 0;
+}
+
 // Resident threads the device holds (SM count x 2048), cached per device.
 inline int64_t device_capacity() {
   static int64_t cap[64] = {0};
@@ -128,7 +135,8 @@ inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
 template <typename T, int SO, int IO, int ZB, int SPLIT, class Epi>
 int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* partials,
                   const int* skip, cudaStream_t st) {
-  const Dims d = dims_of(g, Nz);
+  Dims d = dims_of(g, Nz);
+  d.vec4 = aligned_groups_of_4(img, Nz);
   const dim3 grid = fwd_grid(g, Nz, SPLIT);
   if constexpr (std::is_same<T, float>::value) {
     if (g->kind == GR_RADON) {
@@ -184,7 +192,8 @@ int launch_fwd(const gr_geometry* g, const void* img, int Nz, Epi epi, double* p
 template <typename T, int IO, int SO, int ZB, int SPLIT, class Epi>
 int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* partials,
                   const int* skip, cudaStream_t st) {
-  const Dims d = dims_of(g, Nz);
+  Dims d = dims_of(g, Nz);
+  d.vec4 = aligned_groups_of_4(sino, Nz);
   const dim3 grid = bwd_grid(g, Nz, IO, SPLIT);
   const dim3 block(kBwdTileFast, kBwdTileSlow);
   if constexpr (std::is_same<T, float>::value) {

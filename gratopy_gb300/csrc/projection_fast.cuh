@@ -90,6 +90,17 @@ __device__ __forceinline__ void stage_windows(Window<ZB>& win, const Rec* rec, i
       const bool in = bin >= 0 && bin < (int)d.Ns;
       const float sc = (FAN && in) ? ldg(sdpd + bin) : 1.0f;
       const float* p = prow + (int64_t)bin * ss_;
+      if constexpr (SO == ORDER_C && ZB == 4) {
+        if (d.vec4) {
+          const float4 q = in ? __ldg(reinterpret_cast<const float4*>(p))
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+          win.v[j][0][k] = sc * q.x;
+          win.v[j][1][k] = sc * q.y;
+          win.v[j][2][k] = sc * q.z;
+          win.v[j][3][k] = sc * q.w;
+          continue;
+        }
+      }
 #pragma unroll
       for (int zz = 0; zz < ZB; ++zz)
         win.v[j][zz][k] = (in && zz < zn) ? sc * ldg(p + zz * sz_) : 0.0f;
@@ -459,6 +470,25 @@ fan_bwd_fast(const float* __restrict__ sino, const float* __restrict__ ofs,
 // image are skipped by solving the two linear bound conditions for the rows.
 constexpr int kRayGroup = 4;
 
+// The ZB slices of one pixel, times `scale`: one float4 load when the image
+// is C-ordered and 16-byte aligned in groups of 4 slices, else ZB loads.
+template <int IO, int ZB>
+__device__ __forceinline__ void load_slices(float (&v)[ZB], const float* p, int64_t sz, int zn,
+                                            bool vec4, float scale) {
+  if constexpr (IO == ORDER_C && ZB == 4) {
+    if (vec4) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+      v[0] = q.x * scale;
+      v[1] = q.y * scale;
+      v[2] = q.z * scale;
+      v[3] = q.w * scale;
+      return;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < ZB; ++k) v[k] = k < zn ? ldg(p + k * sz) * scale : 0.0f;
+}
+
 template <int SPLIT>
 struct GroupLayout {
   static constexpr int kGroupsPerWarp = 32 / SPLIT;
@@ -551,8 +581,7 @@ __device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ 
       float pos = fmaf((float)x_low, ox, dd);
       for (int x = x_low; x <= x_high; ++x) {
         float v[ZB];
-#pragma unroll
-        for (int k = 0; k < ZB; ++k) v[k] = k < zn ? ldg(p + k * sz) : 0.0f;
+        load_slices<IO, ZB>(v, p, sz, zn, d.vec4, 1.0f);
 #pragma unroll
         for (int r = 0; r < kRayGroup; ++r) {
           const float w = 1.0f - fabsf(pos - (float)r);
@@ -636,7 +665,14 @@ __device__ __forceinline__ double fan_fwd_fast_tile(const float* __restrict__ im
     int64_t sx, sy, sz;
     img_strides<IO>(d, sx, sy, sz);
     int64_t step_x = sx, step_y = sy;
-    if (!(fabsf(dpx) < fabsf(dpy) && fabsf(dmx) < fabsf(dmy))) {
+    // Rows run along x unless a boundary ray is closer to the x axis than to
+    // the y axis (fanbeam.cl:183-206).  The candidates of a row form the
+    // interval between the two boundary rays only if the wedge between them
+    // does not contain the row direction; the wedge of a group spans 5 bins,
+    // so on coarse detectors it can hold a diagonal, and then the other
+    // orientation is taken when the swapped one would contain its rows.
+    const bool steep = fabsf(dpx) < fabsf(dpy) && fabsf(dmx) < fabsf(dmy);
+    if (!steep && dpx * dmx > 0.0f) {
       float t;
       t = ddx; ddx = ddy; ddy = t;
       t = dx; dx = dy; dy = t;
@@ -678,8 +714,7 @@ __device__ __forceinline__ double fan_fwd_fast_tile(const float* __restrict__ im
         const float r = rcp_approx(t);
         const float u = fmaf(ss, r, -s_mid0);  // xi - (s0 - mid) in bins
         float v[ZB];
-#pragma unroll
-        for (int k = 0; k < ZB; ++k) v[k] = k < zn ? ldg(p + k * sz) * r : 0.0f;
+        load_slices<IO, ZB>(v, p, sz, zn, d.vec4, r);
 #pragma unroll
         for (int q = 0; q < kRayGroup; ++q) {
           const float w = 1.0f - fabsf((float)q - u);
