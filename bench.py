@@ -370,11 +370,11 @@ def extra_batched(device, small=False):
             "timing": "wall clock around the whole solve, synchronised"}
 
 
-def extra_autograd(device):
+def extra_autograd(device, order="F"):
     """Gradient step through Radon projections and an unrolled TV reconstruction.
 
-    16 float32 512 x 512 images (one stack, independent slices), 360 angles in
-    [0, pi), 725 detectors.  loss = ||A x - y||^2 + ||TV_20(A x) - x_true||^2
+    16 float32 512 x 512 images (one stack in ``order``, independent slices),
+    360 angles in [0, pi), 725 detectors.  loss = ||A x - y||^2 + ||TV_20(A x) - x_true||^2
     with TV_20 = 20 primal-dual iterations (mu = 20) checkpointed every 5;
     a step is the forward pass plus ``loss.backward()``.
     """
@@ -388,8 +388,8 @@ def extra_autograd(device):
     ps = gg.ProjectionSettings(device, gg.RADON, (512, 512), 360, n_detectors=725)
     truth = np.stack([random_ellipse_image(SEED + k, (512, 512), count=10, dtype="float32").T
                       for k in range(nz)], -1)
-    x_true = gg.core.empty((512, 512, nz), torch.float32, "F", device)
-    x_true.copy_(torch.from_numpy(np.ascontiguousarray(truth.transpose(2, 1, 0))).permute(2, 1, 0))
+    x_true = gg.core.empty((512, 512, nz), torch.float32, order, device)
+    x_true.copy_(torch.from_numpy(np.ascontiguousarray(truth)))
     y = gg.forwardprojection(x_true, ps)
     gen = torch.Generator(device=device).manual_seed(SEED)
     y += 0.01 * float(y.abs().max()) * torch.randn(y.shape, generator=gen, device=device)
@@ -410,18 +410,20 @@ def extra_autograd(device):
     # the checkpoint replay, 2 per adjoint iteration, A^T for the data term
     projections = 1 + 2 * 20 + 2 * 20 + 2 * 20 + 1
     pa = 512 * 512 * 360 * nz
-    return {"workload": "16 x 512^2 Radon stack, 360 angles [0,pi), 725 detectors; "
-                        "||Ax-y||^2 + ||TV20(Ax)-x||^2, checkpoint every 5, forward+backward",
+    return {"workload": f"16 x 512^2 Radon stack ({order} order), 360 angles [0,pi), 725 "
+                        "detectors; ||Ax-y||^2 + ||TV20(Ax)-x||^2, checkpoint every 5, "
+                        "forward+backward",
             "steps_per_s": 1.0 / t, "ms_per_step": t * 1e3, "projections_per_step": projections,
             "gpixel_angle_per_s": projections * pa / t / 1e9}
 
 
-def extra_large_stack(device, iterations=3, adjoint_iterations=5):
+def extra_large_stack(device, iterations=3, adjoint_iterations=5, order="F"):
     """2048 x 2048 x 64 fan-beam stack: TV primal-dual and its adjoint, per iteration.
 
     1440 angles over [0, 2pi), 2900 detectors, RE = 1000, R = 2000, detector
-    width 2000, automatic image width, mu = 50, slice thickness 1; F order
-    (each slice a plane, 4 slices per thread in the projections).  A full
+    width 2000, automatic image width, mu = 50, slice thickness 1; stack in
+    ``order`` (F: each slice a plane; C: slices fastest, 4 slices per float4
+    load; the projections carry 4 slices per thread either way).  A full
     500-iteration reconstruction with a differentiable backward through the
     last 50 iterations is extrapolated from the measured per-iteration times:
     500 TV iterations + 50 x (replay + adjoint).
@@ -435,7 +437,7 @@ def extra_large_stack(device, iterations=3, adjoint_iterations=5):
     nz = 64
     ps = gg.ProjectionSettings(device, gg.FANBEAM, (2048, 2048), 1440, n_detectors=2900,
                                detector_width=2000.0, R=2000.0, RE=1000.0)
-    vol = random_ellipse_volume(device, (2048, 2048), nz, seed=SEED, order="F")
+    vol = random_ellipse_volume(device, (2048, 2048), nz, seed=SEED, order=order)
     sino = gg.forwardprojection(vol, ps)
     del vol
     nrm = gg.normest(ps, 50)
@@ -457,8 +459,8 @@ def extra_large_stack(device, iterations=3, adjoint_iterations=5):
     pa = 2048 * 2048 * 1440 * nz
     del f, sino
     torch.cuda.empty_cache()
-    return {"workload": "fanbeam 2048^2 x 64 slices float32 F order, 1440 angles, 2900 detectors, "
-                        "RE=1000, R=2000; TV mu=50, slice thickness 1",
+    return {"workload": f"fanbeam 2048^2 x 64 slices float32 {order} order, 1440 angles, "
+                        "2900 detectors, RE=1000, R=2000; TV mu=50, slice thickness 1",
             "tv_ms_per_iteration": t_tv * 1e3,
             "tv_gpixel_angle_per_s": 2 * pa / t_tv / 1e9,
             "backward_ms_per_iteration": t_back_iter * 1e3,
@@ -473,8 +475,15 @@ EXTRAS = {
     "batched": lambda device, ps, res: extra_batched(device),
     "batched_small": lambda device, ps, res: extra_batched(device, small=True),
     "autograd": lambda device, ps, res: extra_autograd(device),
+    "autograd_c": lambda device, ps, res: extra_autograd(device, order="C"),
     "large_stack": lambda device, ps, res: extra_large_stack(device),
+    "large_stack_c": lambda device, ps, res: extra_large_stack(device, order="C"),
 }
+
+
+# the C-ordered large stack is left out of the default run: its x-walk strides
+# 64 x 2048 floats per pixel and runs 3x slower than the F-ordered stack
+DEFAULT_EXTRAS = [e for e in EXTRAS if e != "large_stack_c"]
 
 
 def cpu_baseline_sample(max_seconds=12.0):
@@ -508,7 +517,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the secondary workloads")
     ap.add_argument("--extras", default="all",
-                    help="comma list of secondary workloads: " + ",".join(EXTRAS) + " (or all)")
+                    help="comma list of secondary workloads: " + ",".join(EXTRAS)
+                    + " (or all: every one but large_stack_c)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -594,7 +604,7 @@ def main():
                               "peak_source": "measured: gr_probe_l1_bandwidth (float4 loads, "
                                              "L1-resident buffer)"}
     wanted = [] if args.no_extras else (
-        list(EXTRAS) if args.extras == "all" else [e for e in args.extras.split(",") if e])
+        DEFAULT_EXTRAS if args.extras == "all" else [e for e in args.extras.split(",") if e])
     for name in wanted:
         if name not in EXTRAS:
             raise SystemExit(f"unknown extra workload {name!r}; choose from {', '.join(EXTRAS)}")
