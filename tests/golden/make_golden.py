@@ -1,7 +1,7 @@
 """Generate the golden fixtures of tests/golden/ from the gratopy reference.
 
-Run in a checkout that has the reference at /root/reference (the GPU machine
-never runs this; tests only read the committed outputs):
+Run on a machine that has the reference checked out at /root/reference
+(the tests only read the committed outputs and never run this):
 
     python tests/golden/make_golden.py
 
