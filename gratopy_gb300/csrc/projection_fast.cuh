@@ -579,6 +579,9 @@ __device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ 
       const int x_high = min((int)((c_hi - dd) * ow), Nxx - 1);
       const float* p = img0 + (int64_t)y * step_y + (int64_t)x_low * step_x;
       float pos = fmaf((float)x_low, ox, dd);
+      // two candidates per trip for single slices (measured: 256^2 Radon
+      // forward 43.7 -> 37 us; the fan loop, with its reciprocal, loses)
+#pragma unroll(ZB == 1 ? 2 : 1)
       for (int x = x_low; x <= x_high; ++x) {
         float v[ZB];
         load_slices<IO, ZB>(v, p, sz, zn, d.vec4, 1.0f);
