@@ -423,3 +423,24 @@ def total_variation_sharded(sino_ext, projectionsetting, mu, number_iterations=1
     be = KernelTV(sino_ext, projectionsetting, mu, slice_thickness, stepsize_weighting,
                   norm_estimate, halo.ghost_below, halo.ghost_above)
     return tv_sharded(be, number_iterations, group)
+
+
+# --------------------------------------------------------- batches, sharded
+
+
+def batch_sharded(problems, device=None, group=None, **kwargs):
+    """Solve this rank's share of a heterogeneous batch (no exchange).
+
+    The problems are split over the ranks of ``group`` by
+    :func:`partition_problems`; this rank runs its share as one
+    :class:`~gratopy_gb300.batch.BatchedReconstruction` (``kwargs`` go to
+    it) and returns ``{index: reconstruction}`` for the problems it solved.
+    """
+    from .batch import BatchedReconstruction
+
+    rank, world = _rank_world(group)
+    mine = partition_problems(problems, world)[rank]
+    if not mine:
+        return {}
+    out = BatchedReconstruction([problems[i] for i in mine], device, **kwargs).run()
+    return dict(zip(mine, out))

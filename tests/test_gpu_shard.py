@@ -54,3 +54,21 @@ def test_kernel_tv_one_rank_equals_total_variation(cuda_device):
     a = shard.total_variation_sharded(sino, ps, 10.0, 15, slice_thickness=1.0, norm_estimate=nrm)
     b = gg.total_variation(sino, ps, 10.0, 15, slice_thickness=1.0, norm_estimate=nrm)
     assert torch.equal(a, b)
+
+
+def test_batch_sharded_one_rank_solves_everything(cuda_device):
+    import torch
+
+    from gratopy_gb300 import batch as gb
+    from gratopy_gb300 import shard
+
+    def problems():
+        return gb.heterogeneous_problems(5, seed=4, device=cuda_device, landweber_iterations=4,
+                                         cg_iterations=3, tv_iterations=4, sizes=(32, 48),
+                                         angle_range=(20, 40))
+
+    a = shard.batch_sharded(problems(), cuda_device, normest_iterations=5)
+    b = gb.BatchedReconstruction(problems(), cuda_device, normest_iterations=5).run()
+    assert sorted(a) == list(range(5))
+    for k in range(5):
+        assert torch.equal(a[k], b[k])
