@@ -353,6 +353,7 @@ def extra_batched(device, small=False):
     # shapes (batched backprojection tiles use one thread row per angle set)
     for p in solved:
         p.settings.gr_geometry(np.float32).bwd_split = 1
+        p.settings.gr_geometry(np.float32).sym = 0
     same = [gb.Problem(p.settings, p.sino, p.solver, p.iterations, mu=p.mu,
                        norm_estimate=p.norm_estimate) for p in solved]
     ref = gb.solve_plain(same)

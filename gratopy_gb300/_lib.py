@@ -35,6 +35,8 @@ class GrGeometry(ctypes.Structure):
         ("geo", ctypes.c_double * 11),
         ("fwd_split", ctypes.c_int),
         ("bwd_split", ctypes.c_int),
+        ("sym", ctypes.c_int),
+        ("sym_map", (ctypes.c_int * 6) * 3),
     ]
 
 

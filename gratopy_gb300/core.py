@@ -323,10 +323,25 @@ class ProjectionSettings:
         geo = np.asarray(self.struct["geo_dict"][dtype], dtype=np.float64)
         for i, v in enumerate(geo):
             g.geo[i] = float(v)
+        maps = self.quarter_maps()
+        if maps is not None:
+            g.sym = 4
+            for m, row in enumerate(maps):
+                for k, v in enumerate(row):
+                    g.sym_map[m][k] = int(v)
         self._geom[dtype] = g
         ga = _lib.GrGeometry.from_buffer_copy(g)
         ga.ofs = tables["ofs_adj"].data_ptr()
         self._geom_adj[dtype] = ga
+
+    def quarter_maps(self):
+        """Index maps of a quarter-turn symmetric fan-beam geometry (see
+        :mod:`gratopy_gb300.symmetry`), or None; computed once."""
+        if not hasattr(self, "_quarter"):
+            from .symmetry import fan_quarter_maps
+
+            self._quarter = fan_quarter_maps(self.struct, self.img_shape) if self.is_fan else None
+        return self._quarter
 
     def forward_scale(self, dtype) -> float:
         """Scale the forward kernels apply after the interpolation sums, in their arithmetic.

@@ -117,11 +117,32 @@ inline int bwd_split(const gr_geometry* g, int Nz) {
   return clamp_split(g, 8);
 }
 
+// float32 fan-beam single slices with a quarter-turn symmetric angle set:
+// one block row per base angle, four angles per lane group.
+inline bool use_quarter(const gr_geometry* g, int Nz) {
+  return g->sym == 4 && g->dtype == GR_F32 && g->kind == GR_FANBEAM && Nz == 1 &&
+         g->Na % 4 == 0 && g->Nx == g->Ny;
+}
+
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   const int ZB = zblock(Nz);
   const int group = g->dtype == GR_F32 ? fast::kRayGroup : 1;  // bins per lane group
   const int per_block = (32 / split) * (kFwdBlock / 32) * group;
-  return dim3((g->Ns + per_block - 1) / per_block, g->Na, (Nz + ZB - 1) / ZB);
+  const int angles = use_quarter(g, Nz) ? g->Na / 4 : g->Na;
+  return dim3((g->Ns + per_block - 1) / per_block, angles, (Nz + ZB - 1) / ZB);
+}
+
+inline fast::QuarterMaps quarter_maps(const gr_geometry* g) {
+  fast::QuarterMaps q;
+  for (int m = 0; m < 3; ++m) {
+    q.axx[m] = g->sym_map[m][0];
+    q.axy[m] = g->sym_map[m][1];
+    q.ayx[m] = g->sym_map[m][2];
+    q.ayy[m] = g->sym_map[m][3];
+    q.cx[m] = g->sym_map[m][4];
+    q.cy[m] = g->sym_map[m][5];
+  }
+  return q;
 }
 
 inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
@@ -142,6 +163,10 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
     if (g->kind == GR_RADON) {
       fast::radon_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
           img, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi, partials, skip);
+    } else if (ZB == 1 && use_quarter(g, Nz)) {
+      fast::fan_fwd_quarter<SO, IO, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+          img, static_cast<const float*>(g->ofs), static_cast<const float*>(g->sdpd),
+          fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials, skip);
     } else {
       fast::fan_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
           img, static_cast<const float*>(g->ofs), static_cast<const float*>(g->sdpd),
@@ -258,6 +283,9 @@ inline gr_geometry make_geo(int kind, int dtype, const void* ofs, const void* sd
   g.dtype = dtype;
   g.fwd_split = 0;
   g.bwd_split = 0;
+  g.sym = 0;  // the reference-style entries keep every angle's own geometry
+  for (int m = 0; m < 3; ++m)
+    for (int k = 0; k < 6; ++k) g.sym_map[m][k] = 0;
   g.ofs = ofs;
   g.sdpd = sdpd;
   const int n = kind == GR_RADON ? 6 : 11;

@@ -767,5 +767,173 @@ fan_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs,
   }
 }
 
+// ------------------------------------------------- quarter-turn symmetry
+// When the angles a + m*Na/4 (m = 1, 2, 3) see the pixel grid as angle a sees
+// it after m quarter turns (square image centred on the rotation axis,
+// equispaced full-circle angles; detected on the host), a lane group of the
+// forward projection works on base angle a and, for every candidate pixel P
+// of that angle, applies the interpolation weights of P (one reciprocal and
+// four hat evaluations) to the four pixels S_m^-1 P: sino[s, a + m Na/4] is
+// the projection of the turned image at angle a.  Index maps: pixel (x, y)
+// of the base angle is pixel (cx + axx x + axy y, cy + ayx x + ayy y) for
+// angle a + m Na/4.
+struct QuarterMaps {
+  int axx[3], axy[3], ayx[3], ayy[3], cx[3], cy[3];
+};
+
+template <int SO, int IO, int SPLIT, class Epi>
+__device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__ img,
+                                                       const float* __restrict__ ofs,
+                                                       const float* __restrict__ sdpd,
+                                                       FanGeo<float> g, Dims d, QuarterMaps qm,
+                                                       Epi epi, uint3 bid) {
+  constexpr int kOrbit = 4;
+  const GroupLayout<SPLIT> L(bid);
+  const int64_t s0 = L.s0;
+  const int64_t a = bid.y;              // base angle in [0, Na/4)
+  const int64_t quarter = d.Na / kOrbit;
+  const bool active = s0 < d.Ns;
+  float acc[kOrbit][kRayGroup];
+#pragma unroll
+  for (int m = 0; m < kOrbit; ++m)
+#pragma unroll
+    for (int q = 0; q < kRayGroup; ++q) acc[m][q] = 0.0f;
+  const float R = g.R;
+  if (active) {
+    float midx = g.midx, midy = g.midy;
+    const float* o = ofs + 8 * a;
+    float dx = o[0], dy = o[1], qx = o[2], qy = o[3];
+    const float d0x = o[4], d0y = o[5];
+    const float sr = (float)(int)s0;
+    const float fp = -g.mid_det + sr + (float)kRayGroup;
+    const float fm = -g.mid_det + sr - 1.0f;
+    float dpx = d0x + dx * fp - qx, dpy = d0y + dy * fp - qy;
+    float dmx = d0x + dx * fm - qx, dmy = d0y + dy * fm - qy;
+    float ddx = (d0x - qx) / (R * R), ddy = (d0y - qy) / (R * R);
+    const float xx2 = g.delta_xi * g.delta_xi;
+    dx /= xx2;
+    dy /= xx2;
+    const float RE = g.RE * (1.0f / R);
+    int Nyy = (int)d.Ny, Nxx = (int)d.Nx;
+    int64_t sx, sy, sz;
+    img_strides<IO>(d, sx, sy, sz);
+    // element steps of the turned pixels along the array's x and y axes
+    // (32-bit: a single slice of at most 2^31 pixels)
+    int mstep_x[kOrbit - 1], mstep_y[kOrbit - 1], mbase[kOrbit - 1];
+#pragma unroll
+    for (int m = 0; m < kOrbit - 1; ++m) {
+      mstep_x[m] = (int)(qm.axx[m] * sx + qm.ayx[m] * sy);
+      mstep_y[m] = (int)(qm.axy[m] * sx + qm.ayy[m] * sy);
+      mbase[m] = (int)(qm.cx[m] * sx + qm.cy[m] * sy);
+    }
+    int64_t step_x = sx, step_y = sy;
+    const bool steep = fabsf(dpx) < fabsf(dpy) && fabsf(dmx) < fabsf(dmy);
+    const bool swap = !steep && dpx * dmx > 0.0f;
+    if (swap) {
+      float t;
+      t = ddx; ddx = ddy; ddy = t;
+      t = dx; dx = dy; dy = t;
+      t = qx; qx = qy; qy = t;
+      t = dpx; dpx = dpy; dpy = t;
+      t = dmx; dmx = dmy; dmy = t;
+      t = midx; midx = midy; midy = t;
+      Nyy = (int)d.Nx;
+      Nxx = (int)d.Ny;
+      step_x = sy;
+      step_y = sx;
+#pragma unroll
+      for (int m = 0; m < kOrbit - 1; ++m) {
+        const int t2 = mstep_x[m];
+        mstep_x[m] = mstep_y[m];
+        mstep_y[m] = t2;
+      }
+    }
+    dpx /= dpy;
+    dmx /= dmy;
+    if (qy * (dmx - dpx) < 0.0f) {
+      float t = dpx; dpx = dmx; dmx = t;
+    }
+    const float s_mid0 = sr - g.mid_det;
+    const float qxm = qx + midx, yc = -midy - qy;
+    const float hi_lim = (float)(Nxx - 1);
+    const float t_c = RE - ddx * midx - ddy * midy;
+    const float s_c = -dx * midx - dy * midy;
+    int y0, y1;
+    row_range(fmaf(dmx, yc, qxm), dmx, fmaf(dpx, yc, qxm), dpx, hi_lim, Nyy, y0, y1);
+    const int ys = y0 + L.lane_group;
+    float yf = (float)ys;
+    for (int y = ys; y <= y1; y += SPLIT, yf += (float)SPLIT) {
+      const float yrel = yf + yc;
+      const int xhi = (int)floorf(fminf(hi_lim, fmaf(dpx, yrel, qxm)));
+      const int xlo = (int)ceilf(fmaxf(0.0f, fmaf(dmx, yrel, qxm)));
+      const float xlf = (float)xlo;
+      float t = fmaf(ddx, xlf, fmaf(ddy, yf, t_c));
+      float ss = fmaf(dx, xlf, fmaf(dy, yf, s_c));
+      const int stp = (int)step_x;
+      int o0 = (int)(y * step_y + xlo * step_x);
+      int om[kOrbit - 1];
+#pragma unroll
+      for (int m = 0; m < kOrbit - 1; ++m) om[m] = mbase[m] + y * mstep_y[m] + xlo * mstep_x[m];
+      for (int x = xlo; x <= xhi; ++x) {
+        const float r = rcp_approx(t);
+        const float u = fmaf(ss, r, -s_mid0);
+        float v[kOrbit];
+        v[0] = ldg(img + o0) * r;
+#pragma unroll
+        for (int m = 0; m < kOrbit - 1; ++m) v[m + 1] = ldg(img + om[m]) * r;
+#pragma unroll
+        for (int q = 0; q < kRayGroup; ++q) {
+          const float w = 1.0f - fabsf((float)q - u);
+          if (w > 0.0f) {
+#pragma unroll
+            for (int m = 0; m < kOrbit; ++m) acc[m][q] = fmaf(w, v[m], acc[m][q]);
+          }
+        }
+        o0 += stp;
+#pragma unroll
+        for (int m = 0; m < kOrbit - 1; ++m) om[m] += mstep_x[m];
+        t += ddx;
+        ss += dx;
+      }
+    }
+  }
+  if (SPLIT > 1) {
+#pragma unroll
+    for (int m = 0; m < kOrbit; ++m) warp_reduce_rows<SPLIT>(acc[m]);
+  }
+  double part = 0.0;
+  if (active && L.lane_group == 0) {
+#pragma unroll
+    for (int q = 0; q < kRayGroup; ++q) {
+      const int64_t s = s0 + q;
+      if (s < d.Ns) {
+        const float sc = sdpd[s] / g.delta_xi * g.delta_x / R;
+#pragma unroll
+        for (int m = 0; m < kOrbit; ++m) {
+          const int64_t am = a + m * quarter;
+          part += epi(s, am, 0, sino_index<SO>(s, am, 0, d), acc[m][q] * sc);
+        }
+      }
+    }
+  }
+  return part;
+}
+
+template <int SO, int IO, int SPLIT, class Epi>
+__global__ void __launch_bounds__(kFwdBlock)
+fan_fwd_quarter(const float* __restrict__ img, const float* __restrict__ ofs,
+                const float* __restrict__ sdpd, FanGeo<float> g, Dims d, QuarterMaps qm, Epi epi,
+                double* __restrict__ partials, const int* __restrict__ skip) {
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const double part =
+      fan_fwd_quarter_tile<SO, IO, SPLIT, Epi>(img, ofs, sdpd, g, d, qm, epi, blockIdx);
+  if (Epi::kReduce) {
+    double t = block_sum(part, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0)
+      partials[bid_linear()] = t;
+  }
+}
+
 }  // namespace fast
 }  // namespace gr

@@ -1,0 +1,85 @@
+"""Quarter-turn symmetry of fan-beam angle sets.
+
+With a square image centred on the rotation axis and angles equispaced over
+the full circle in a multiple of 4, the angle a + m*Na/4 sees the pixel grid
+exactly as angle a sees it after a quarter turn (m = 1), a half turn (2) or a
+three-quarter turn (3).  Then, for every detector bin s,
+
+    sino[s, a + m Na/4] = sum_P img(S_m^-1 P) K(a, P; s),
+
+so the forward projection can evaluate the interpolation weights K of a
+candidate pixel once for angle a and apply them to four pixels, one per
+angle of the quarter-turn orbit.  This module finds the index maps S_m^-1 by
+evaluating the geometry (detector coordinate and distance weight of the
+fan-beam kernels, fanbeam.cl:290-391) in float64 for every base angle on
+sample pixels, and returns None when any check fails.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+# the 8 signed permutations of the plane, as (S00, S01, S10, S11)
+_MAPS = [(1, 0, 0, 1), (-1, 0, 0, -1), (0, -1, 1, 0), (0, 1, -1, 0),
+         (-1, 0, 0, 1), (1, 0, 0, -1), (0, 1, 1, 0), (0, -1, -1, 0)]
+
+
+def _sample_pixels(N: int, rng_seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    if N <= 48:
+        x, y = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
+        return x.ravel().astype(np.float64), y.ravel().astype(np.float64)
+    rng = np.random.default_rng(rng_seed)
+    x = np.concatenate([[0, 0, N - 1, N - 1, N // 2], rng.integers(0, N, 251)])
+    y = np.concatenate([[0, N - 1, 0, N - 1, N // 3], rng.integers(0, N, 251)])
+    return x.astype(np.float64), y.astype(np.float64)
+
+
+def fan_quarter_maps(struct, img_shape, atol_bins: float = 1e-6, rtol_t: float = 1e-9):
+    """Index maps of the quarter-turn orbit of a fan-beam geometry, or None.
+
+    Returns a list of three tuples ``(Axx, Axy, Ayx, Ayy, Cx, Cy)``, one per
+    m = 1, 2, 3: the pixel of array indices ``(x, y)`` seen by base angle a
+    corresponds, for angle a + m*Na/4, to the pixel
+    ``(Cx + Axx*x + Axy*y, Cy + Ayx*x + Ayy*y)``.
+    """
+    Nx, Ny = (int(v) for v in img_shape)
+    ofs = np.asarray(struct["ofs_dict"][np.dtype("float64")], dtype=np.float64)
+    geo = np.asarray(struct["geo_dict"][np.dtype("float64")], dtype=np.float64)
+    Na = ofs.shape[1]
+    if Nx != Ny or Na < 4 or Na % 4 != 0:
+        return None
+    c = (Nx - 1) * 0.5
+    if geo[3] != c or geo[4] != c:  # image not centred on the rotation axis
+        return None
+    R, RE, dxi, mid_det = geo[0], geo[1], geo[2], geo[5]
+    Q = Na // 4
+    px, py = _sample_pixels(Nx)
+    px, py = px - c, py - c
+
+    def u_t(a, X, Y):
+        XD, YD, Qx, Qy, Dx0, Dy0 = (ofs[k, a][:, None] for k in range(6))
+        t = ((Dx0 - Qx) * X + (Dy0 - Qy) * Y) / (R * R) + RE / R
+        ss = (XD * X + YD * Y) / (dxi * dxi)
+        return ss / t + mid_det, t
+
+    base = np.arange(Q)
+    maps = []
+    for m in (1, 2, 3):
+        u1, t1 = u_t(base + m * Q, px[None, :], py[None, :])
+        found = None
+        for S in _MAPS:
+            X = S[0] * px + S[1] * py
+            Y = S[2] * px + S[3] * py
+            u0, t0 = u_t(base, X[None, :], Y[None, :])
+            if (np.all(np.abs(u1 - u0) <= atol_bins)
+                    and np.all(np.abs(t1 - t0) <= rtol_t * np.abs(t1))):
+                found = S
+                break
+        if found is None:
+            return None
+        # the load for angle a + m Q at base candidate P is img(S^-1 P), S^-1 = S^T
+        Axx, Axy, Ayx, Ayy = found[0], found[2], found[1], found[3]
+        Cx = int(round(c * (1 - Axx - Axy)))
+        Cy = int(round(c * (1 - Ayx - Ayy)))
+        maps.append((Axx, Axy, Ayx, Ayy, Cx, Cy))
+    return maps

@@ -61,6 +61,15 @@ typedef struct gr_geometry {
    * projection and angle groups per pixel in the backprojection; each must
    * be 1, 2, 4 or 8.  Chosen by the autotuner. */
   int fwd_split, bwd_split;
+  /* Quarter-turn symmetry (no counterpart in the reference): 4 when the
+   * angles a + m*Na/4 see the (square, centred) pixel grid as angle a sees it
+   * after m quarter turns, else 0.  sym_map[m-1] = (axx, axy, ayx, ayy, cx,
+   * cy): pixel (x, y) of angle a is pixel (cx + axx x + axy y, cy + ayx x +
+   * ayy y) of angle a + m*Na/4.  The float32 fan-beam forward projection of
+   * single slices then shares each pixel's interpolation weights across the
+   * four angles.  Set by the Python layer after checking the geometry. */
+  int sym;
+  int sym_map[3][6];
 } gr_geometry;
 
 GR_API const char* gr_error_string(int code);

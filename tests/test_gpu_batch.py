@@ -68,9 +68,11 @@ def test_batched_matches_per_call(cuda_device):
     results = runner.run()
     for pr, got in zip(problems, results):
         ps = pr.settings
-        # the per-call form with the batched launch shape (one thread row per
-        # angle set in the backprojection), so both add in the same order
+        # the per-call form with the batched launch shapes (one thread row per
+        # angle set in the backprojection, every angle's own forward), so both
+        # add in the same order
         ps.gr_geometry(np.float32).bwd_split = 1
+        ps.gr_geometry(np.float32).sym = 0
         if pr.solver in ("landweber", "tv"):
             want_n = gg.normest(ps, 20, x0=pr.normest_x0)
             assert abs(pr.norm_estimate - want_n) <= 1e-12 * want_n

@@ -94,7 +94,8 @@ def test_degenerate_problems_in_a_batch(cuda_device):
     out = gb.BatchedReconstruction(problems, cuda_device).run()
     for pr, got in zip(problems, out):
         ps = pr.settings
-        ps.gr_geometry(np.float32).bwd_split = 1  # the batched backprojection's launch shape
+        ps.gr_geometry(np.float32).bwd_split = 1  # the batched launch shapes
+        ps.gr_geometry(np.float32).sym = 0
         if pr.solver == "landweber":
             want = gg.landweber(pr.sino, ps, 4, norm_estimate=pr.norm_estimate)
         elif pr.solver == "cg":
