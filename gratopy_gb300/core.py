@@ -489,60 +489,44 @@ def _event(device):
     return ev
 
 
+def _project(entry, out, inp, out_order, in_order, ps):
+    """One projection through the settings' geometry descriptor: the tuned
+    launch shape and, for quarter-turn symmetric fan-beam angle sets, the
+    orbit-sharing forward kernel apply."""
+    g = ps.gr_geometry(_np_dtype(out.dtype))
+    with torch.cuda.device(out.device):
+        _lib.call(entry, ctypes.byref(g), _ptr(out), _ptr(inp), _nz(out), _oflag(out_order),
+                  _oflag(in_order), _stream_ptr(out.device))
+        return _event(out.device)
+
+
 def radon(sino, img, projectionsetting, wait_for=[]):
-    """Radon forward projection into ``sino`` (gratopy.py:258-316); returns a CUDA event."""
+    """Radon forward projection into ``sino`` (gratopy.py:258-316); returns a CUDA event.
+
+    The C library also has the reference kernel's own argument list
+    (``gr_radon_fwd``: ofs table, geometry vector, shapes) for callers
+    without a settings object; this form passes the settings' descriptor.
+    """
     io, so = _prepare(img, sino, projectionsetting)
-    ps = projectionsetting
-    dtype = _np_dtype(sino.dtype)
-    t = ps.device_tables(dtype)
-    geo = (ctypes.c_double * 6)(*np.asarray(ps.struct["geo_dict"][dtype], dtype=np.float64))
-    with torch.cuda.device(sino.device):
-        _lib.call("gr_radon_fwd", _ptr(sino), _ptr(img), _ptr(t["ofs"]), geo, _dt(sino),
-                  ps.sinogram_shape[0], ps.sinogram_shape[1], _nz(sino), _oflag(so), _oflag(io),
-                  _stream_ptr(sino.device))
-        return _event(sino.device)
+    return _project("gr_forward", sino, img, so, io, projectionsetting)
 
 
 def radon_ad(img, sino, projectionsetting, wait_for=[]):
     """Radon backprojection into ``img`` (gratopy.py:319-377); returns a CUDA event."""
     io, so = _prepare(img, sino, projectionsetting)
-    ps = projectionsetting
-    dtype = _np_dtype(sino.dtype)
-    t = ps.device_tables(dtype)
-    geo = (ctypes.c_double * 6)(*np.asarray(ps.struct["geo_dict"][dtype], dtype=np.float64))
-    with torch.cuda.device(img.device):
-        _lib.call("gr_radon_bwd", _ptr(img), _ptr(sino), _ptr(t["ofs"]), geo, _dt(img),
-                  ps.img_shape[0], ps.img_shape[1], _nz(img), _oflag(io), _oflag(so),
-                  _stream_ptr(img.device))
-        return _event(img.device)
+    return _project("gr_backward", img, sino, io, so, projectionsetting)
 
 
 def fanbeam(sino, img, projectionsetting, wait_for=[]):
     """Fan-beam forward projection into ``sino`` (gratopy.py:581-640)."""
     io, so = _prepare(img, sino, projectionsetting)
-    ps = projectionsetting
-    dtype = _np_dtype(sino.dtype)
-    t = ps.device_tables(dtype)
-    geo = (ctypes.c_double * 11)(*np.asarray(ps.struct["geo_dict"][dtype], dtype=np.float64))
-    with torch.cuda.device(sino.device):
-        _lib.call("gr_fan_fwd", _ptr(sino), _ptr(img), _ptr(t["ofs"]), _ptr(t["sdpd"]), geo,
-                  _dt(sino), ps.sinogram_shape[0], ps.sinogram_shape[1], _nz(sino), _oflag(so),
-                  _oflag(io), _stream_ptr(sino.device))
-        return _event(sino.device)
+    return _project("gr_forward", sino, img, so, io, projectionsetting)
 
 
 def fanbeam_ad(img, sino, projectionsetting, wait_for=[]):
     """Fan-beam backprojection into ``img`` (gratopy.py:643-703)."""
     io, so = _prepare(img, sino, projectionsetting)
-    ps = projectionsetting
-    dtype = _np_dtype(sino.dtype)
-    t = ps.device_tables(dtype)
-    geo = (ctypes.c_double * 11)(*np.asarray(ps.struct["geo_dict"][dtype], dtype=np.float64))
-    with torch.cuda.device(img.device):
-        _lib.call("gr_fan_bwd", _ptr(img), _ptr(sino), _ptr(t["ofs"]), _ptr(t["sdpd"]), geo,
-                  _dt(img), ps.img_shape[0], ps.img_shape[1], _nz(img), _oflag(io), _oflag(so),
-                  _stream_ptr(img.device))
-        return _event(img.device)
+    return _project("gr_backward", img, sino, io, so, projectionsetting)
 
 
 def forwardprojection(img, projectionsetting, sino=None, wait_for=[]):

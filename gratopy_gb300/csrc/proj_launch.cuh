@@ -9,6 +9,20 @@
 namespace gr {
 namespace launch {
 
+// A quarter-turn map must send the N x N grid onto itself: a signed
+// permutation of (x, y) whose offsets keep two opposite corners inside.
+inline bool valid_quarter_map(const int* m, int N) {
+  auto unit = [](int v) { return v == 1 || v == -1; };
+  const bool perm = (unit(m[0]) && m[1] == 0 && m[2] == 0 && unit(m[3])) ||
+                    (m[0] == 0 && unit(m[1]) && unit(m[2]) && m[3] == 0);
+  if (!perm) return false;
+  const int64_t last = N - 1;
+  const int64_t x0 = m[4], y0 = m[5];
+  const int64_t x1 = m[4] + (int64_t)(m[0] + m[1]) * last;
+  const int64_t y1 = m[5] + (int64_t)(m[2] + m[3]) * last;
+  auto in = [&](int64_t v) { return v >= 0 && v <= last; };
+  return in(x0) && in(y0) && in(x1) && in(y1);
+}
 
 inline int check_geometry(const gr_geometry* g) {
   if (g == nullptr || g->ofs == nullptr) return GR_ERR_ARG;
@@ -16,6 +30,11 @@ inline int check_geometry(const gr_geometry* g) {
   if (!valid_dtype(g->dtype)) return GR_ERR_ARG;
   if (g->kind == GR_FANBEAM && g->sdpd == nullptr) return GR_ERR_ARG;
   if (g->Nx <= 0 || g->Ny <= 0 || g->Ns <= 0 || g->Na <= 0) return GR_ERR_SHAPE;
+  if (g->sym != 0) {
+    if (g->sym != 4 || g->Nx != g->Ny) return GR_ERR_ARG;
+    for (int m = 0; m < 3; ++m)
+      if (!valid_quarter_map(g->sym_map[m], g->Nx)) return GR_ERR_ARG;
+  }
   if (g->Na > 65535) return GR_ERR_TOO_BIG;
   return GR_OK;
 }
@@ -118,10 +137,12 @@ inline int bwd_split(const gr_geometry* g, int Nz) {
 }
 
 // float32 fan-beam single slices with a quarter-turn symmetric angle set:
-// one block row per base angle, four angles per lane group.
+// one block row per base angle, four angles per lane group.  The kernel
+// keeps pixel offsets in 32 bits, so the slice must hold fewer than 2^31
+// pixels.
 inline bool use_quarter(const gr_geometry* g, int Nz) {
   return g->sym == 4 && g->dtype == GR_F32 && g->kind == GR_FANBEAM && Nz == 1 &&
-         g->Na % 4 == 0 && g->Nx == g->Ny;
+         g->Na % 4 == 0 && g->Nx == g->Ny && (int64_t)g->Nx * g->Ny <= INT32_MAX;
 }
 
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {

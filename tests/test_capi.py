@@ -61,6 +61,29 @@ def test_host_only_entry_points(library):
     g.kind = 7
     assert lib.gr_forward(ctypes.byref(g), None, None, 1, 0, 0, None) == 1
     assert lib.gr_radon_fwd(None, None, None, None, 0, 1, 1, 1, 0, 0, None) == 1
+    # quarter-turn maps are checked before the angle-count limit, so a
+    # geometry with 70000 angles is rejected either way (1: bad maps, 4: too
+    # many angles) and nothing reaches a launch
+    fake = ctypes.c_void_p(64)
+    q = _lib.GrGeometry()
+    q.kind, q.dtype, q.Nx, q.Ny, q.Ns, q.Na = 1, 0, 8, 8, 4, 70000
+    q.ofs, q.sdpd = fake, fake
+    turn = [(0, -1, 1, 0, 7, 0), (-1, 0, 0, -1, 7, 7), (0, 1, -1, 0, 0, 7)]
+
+    def forward_rc(sym, maps):
+        q.sym = sym
+        for m, row in enumerate(maps):
+            for k, v in enumerate(row):
+                q.sym_map[m][k] = v
+        return lib.gr_forward(ctypes.byref(q), fake, fake, 1, 0, 0, None)
+
+    assert forward_rc(4, turn) == 4
+    assert forward_rc(0, [(0,) * 6] * 3) == 4
+    assert forward_rc(3, turn) == 1
+    assert forward_rc(4, [turn[0], turn[1], (0, 1, -1, 0, 0, 8)]) == 1  # leaves the grid
+    assert forward_rc(4, [turn[0], (1, 1, 0, -1, 0, 7), turn[2]]) == 1  # not a permutation
+    q.Ny = 9
+    assert forward_rc(4, turn) == 1  # not square
     assert lib.gr_forward_partials(None, 1) == 0
     # batched descriptors: binding layout equals the library's
     assert lib.gr_batch_problem_size() == ctypes.sizeof(_lib.GrBatchProblem)

@@ -52,7 +52,9 @@ def test_quarter_forward(cuda_device, name, order):
     shared = _forward(ps, img, order, 4, cuda_device)
     direct = _forward(ps, img, order, 0, cuda_device)
     assert rel_l2(shared, ref) < 1e-5
-    assert rel_l2(shared, direct) < 1e-6
+    # float32 sums of a few hundred terms in another order (the turned
+    # image's rows are walked along the base angle's axis)
+    assert rel_l2(shared, direct) < 4e-6
 
 
 @pytest.mark.parametrize("name", ["plain", "shifted_detector"])
