@@ -565,9 +565,12 @@ def main():
     Nx, Ny = ps.img_shape
     compulsory = (Nx * Ny + Ns * Na) * 4
     fwd, bwd = statistics.mean(res["t_fwd"]), statistics.mean(res["t_bwd"])
-    # single fan-beam slices with quarter-turn maps run the orbit-sharing forward
-    fwd_name = "fan_fwd_quarter" if ps.gr_geometry(np.float32).sym == 4 else "fan_fwd_fast"
-    dom, t_dom = (fwd_name, fwd) if fwd >= bwd else ("fan_bwd_fast", bwd)
+    # single fan-beam slices with quarter-turn maps run the orbit kernels (the
+    # backprojection's orbits need an even side)
+    quarter = ps.gr_geometry(np.float32).sym == 4
+    fwd_name = "fan_fwd_quarter" if quarter else "fan_fwd_fast"
+    bwd_name = "fan_bwd_orbit" if quarter and Nx % 2 == 0 else "fan_bwd_fast"
+    dom, t_dom = (fwd_name, fwd) if fwd >= bwd else (bwd_name, bwd)
     achieved = compulsory / t_dom / 1e9
     # DRAM traffic and issue utilisation of the dominant kernel from the
     # committed ncu summary of this workload (not measured in this run)

@@ -116,8 +116,13 @@ inline int fwd_split(const gr_geometry* g, int Nz) {
   return clamp_split(g, 8);
 }
 
+inline bool use_quarter_bwd(const gr_geometry* g, int Nz);
+
 inline int bwd_split(const gr_geometry* g, int Nz) {
   if (valid_split(g->bwd_split)) return clamp_split(g, g->bwd_split);
+  // orbit backprojection: 8 angle groups measured fastest or within 1% of it
+  // from 128^2 to 2048^2 (360 to 1440 angles)
+  if (use_quarter_bwd(g, Nz)) return 8;
   if (g->dtype == GR_F32) {
     // float32 tiles stage detector windows per block, so angles are split
     // over thread rows only when the image alone cannot fill 40% of the
@@ -145,6 +150,34 @@ inline bool use_quarter(const gr_geometry* g, int Nz) {
          g->Na % 4 == 0 && g->Nx == g->Ny && (int64_t)g->Nx * g->Ny <= INT32_MAX;
 }
 
+// Backprojection over quarter-turn pixel orbits: the first map is a turn by
+// a quarter about the image centre and the others are its powers, the side
+// is even (the quadrant x, y < N/2 then holds one pixel of every orbit),
+// and a slice of the sinogram has fewer than 2^31 values (32-bit offsets).
+inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
+  if (!use_quarter(g, Nz) || g->Nx % 2 != 0) return false;
+  if ((int64_t)g->Ns * g->Na > INT32_MAX) return false;
+  const int* m1 = g->sym_map[0];
+  if (m1[0] != 0 || m1[3] != 0 || m1[1] * m1[2] != -1) return false;
+  // apply the first map after an affine map (axx, axy, ayx, ayy, cx, cy)
+  auto after_m1 = [&](const int* f, int* out) {
+    out[0] = m1[0] * f[0] + m1[1] * f[2];
+    out[1] = m1[0] * f[1] + m1[1] * f[3];
+    out[2] = m1[2] * f[0] + m1[3] * f[2];
+    out[3] = m1[2] * f[1] + m1[3] * f[3];
+    out[4] = m1[4] + m1[0] * f[4] + m1[1] * f[5];
+    out[5] = m1[5] + m1[2] * f[4] + m1[3] * f[5];
+  };
+  int m2[6], m3[6], m4[6];
+  after_m1(m1, m2);
+  after_m1(m2, m3);
+  after_m1(m3, m4);
+  const int id[6] = {1, 0, 0, 1, 0, 0};
+  for (int k = 0; k < 6; ++k)
+    if (m2[k] != g->sym_map[1][k] || m3[k] != g->sym_map[2][k] || m4[k] != id[k]) return false;
+  return true;
+}
+
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   const int ZB = zblock(Nz);
   const int group = g->dtype == GR_F32 ? fast::kRayGroup : 1;  // bins per lane group
@@ -167,6 +200,10 @@ inline fast::QuarterMaps quarter_maps(const gr_geometry* g) {
 }
 
 inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
+  if (use_quarter_bwd(g, Nz)) {  // 32 x (8 / split) tiles of the quadrant x, y < N/2
+    const int half = g->Nx / 2, rows = kBwdTileSlow / split;
+    return dim3((half + kBwdTileFast - 1) / kBwdTileFast, (half + rows - 1) / rows, 1);
+  }
   const int ZB = zblock(Nz);
   const int fast = io == ORDER_F ? g->Nx : g->Ny;
   const int slow = io == ORDER_F ? g->Ny : g->Nx;
@@ -247,7 +284,11 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
     // blocks (a 512^2 image then fits in one wave of resident blocks)
     constexpr int PY = (SPLIT == 1 && ZB == 1) ? 2 : 1;
     const dim3 fblock(kBwdTileFast, kBwdTileSlow / PY);
-    if (g->kind == GR_RADON) {
+    if (ZB == 1 && use_quarter_bwd(g, Nz)) {
+      fast::fan_bwd_orbit<IO, SO, SPLIT, Epi><<<grid, block, 0, st>>>(
+          sino, static_cast<const float*>(g->ofs), static_cast<const float*>(g->sdpd),
+          fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials, skip);
+    } else if (g->kind == GR_RADON) {
       fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, fblock, 0, st>>>(
           sino, static_cast<const float*>(g->ofs), d, epi, partials, skip);
     } else {

@@ -919,6 +919,132 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
   return part;
 }
 
+// Backprojection over quarter-turn pixel orbits.  With the maps powers of
+// one quarter turn A (A_m = A^m about the image centre, N even) the pixels
+// P_k = A^k P_0 satisfy u(a + j Na/4, P_k) = u(a, P_{k-j mod 4}) for the
+// detector coordinate and the distance weight alike.  A thread owns the
+// orbit of one pixel P_0 of the quadrant x, y < N/2: for a base angle a in
+// [0, Na/4) it evaluates the geometry of its four pixels once and applies
+// each to the four sinogram rows a + j Na/4, i.e. one reciprocal, one floor
+// and two sdpd loads serve four pixel-angles.  The sinogram values are read
+// directly (the rows of the four angles are L1/L2 resident; no staging, no
+// barrier in the angle loop).  The G thread groups of a block take
+// interleaved base angles and are added in a fixed order at the end.
+template <int IO, int SO, int G, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
+              const float* __restrict__ sdpd, FanGeo<float> gg, Dims d, QuarterMaps qm,
+              Epi epi, double* __restrict__ partials, const int* __restrict__ skip) {
+  constexpr int kOrbit = 4;
+  constexpr int kRowsT = kBwdTileSlow / G;  // quadrant rows of the block tile
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const int lane = threadIdx.x, trow = threadIdx.y;
+  const int grp = trow / kRowsT, trow_t = trow % kRowsT;
+  const int half = (int)(d.Nx / 2);
+  const int Q = (int)(d.Na / kOrbit);
+  const int px0 = (int)blockIdx.x * kBwdTileFast + lane;
+  const int py0 = (int)blockIdx.y * kRowsT + trow_t;
+  const bool own = px0 < half && py0 < half;
+  int ox[kOrbit], oy[kOrbit];
+  ox[0] = px0;
+  oy[0] = py0;
+#pragma unroll
+  for (int m = 0; m < kOrbit - 1; ++m) {
+    ox[m + 1] = qm.cx[m] + qm.axx[m] * px0 + qm.axy[m] * py0;
+    oy[m + 1] = qm.cy[m] + qm.ayx[m] * px0 + qm.ayy[m] * py0;
+  }
+  float pxs[kOrbit], pys[kOrbit];
+#pragma unroll
+  for (int i = 0; i < kOrbit; ++i) {
+    pxs[i] = (float)ox[i] - gg.midx;
+    pys[i] = (float)oy[i] - gg.midy;
+  }
+  const float R = gg.R;
+  const float R_sqr_inv = 1.0f / (R * R);
+  const float dxi_sqr_inv = 1.0f / (gg.delta_xi * gg.delta_xi);
+  const float mid_det = gg.mid_det;
+  int64_t ss_, sa_, sz_;
+  sino_strides<SO>(d, ss_, sa_, sz_);
+  const int ss = (int)ss_, sa = (int)sa_;  // a slice of fewer than 2^31 values
+  const int Ns = (int)d.Ns;
+  float acc[kOrbit];
+#pragma unroll
+  for (int k = 0; k < kOrbit; ++k) acc[k] = 0.0f;
+  // angle weight / R of the rows a + j Q, rounded as the reference does (a
+  // reciprocal multiply would move every weight by up to an ulp in the same
+  // direction, which CG amplifies): lane 4k + j divides for the k-th of the
+  // next 8 base angles of this group, the values reach the other lanes by
+  // shuffle (a warp shares its thread row, hence its group)
+  float wdiv = 0.0f;
+  int chunk = 0;
+  for (int a = grp; a < Q; a += G, ++chunk) {
+    if ((chunk & 7) == 0) {
+      const int ak = a + (lane >> 2) * G;
+      wdiv = ak < Q ? ldg(ofs + 8 * (ak + (lane & 3) * Q) + 6) / R : 0.0f;
+    }
+    const float* o = ofs + 8 * a;
+    const float qx = ldg(o + 2), qy = ldg(o + 3);
+    const float ddx = (ldg(o + 4) - qx) * R_sqr_inv, ddy = (ldg(o + 5) - qy) * R_sqr_inv;
+    const float dx = ldg(o) * dxi_sqr_inv, dy = ldg(o + 1) * dxi_sqr_inv;
+    const float tz = -fmaf(ddx, qx, ddy * qy), sz = -fmaf(dx, qx, dy * qy);
+    float wj[kOrbit];
+    const float* row[kOrbit];
+#pragma unroll
+    for (int j = 0; j < kOrbit; ++j) {
+      wj[j] = __shfl_sync(0xffffffffu, wdiv, ((chunk & 7) << 2) + j);
+      row[j] = sino + (a + j * Q) * sa;
+    }
+#pragma unroll
+    for (int i = 0; i < kOrbit; ++i) {
+      const float t = fmaf(ddx, pxs[i], fmaf(ddy, pys[i], tz));
+      const float s = fmaf(dx, pxs[i], fmaf(dy, pys[i], sz));
+      const float inv = rcp_approx(t);
+      const float xi = fmaf(s, inv, mid_det);
+      const float fl = floorf(xi);
+      const float fr = xi - fl;
+      const int xm = (int)fl;
+      // bins outside the detector contribute nothing; their reads go to bin 0
+      const bool okm = (unsigned)xm < (unsigned)Ns;
+      const bool okp = (unsigned)(xm + 1) < (unsigned)Ns;
+      const int im = okm ? xm : 0, ip = okp ? xm + 1 : 0;
+      const float Wm = okm ? (1.0f - fr) * inv * ldg(sdpd + im) : 0.0f;
+      const float Wp = okp ? fr * inv * ldg(sdpd + ip) : 0.0f;
+#pragma unroll
+      for (int j = 0; j < kOrbit; ++j) {
+        const float v = fmaf(Wp, ldg(row[j] + ip * ss), Wm * ldg(row[j] + im * ss));
+        acc[(i + j) % kOrbit] = fmaf(wj[j], v, acc[(i + j) % kOrbit]);
+      }
+    }
+  }
+  // fixed-order combination of the G angle groups
+  if constexpr (G > 1) {
+    __shared__ float cred[kBwdTileSlow][kOrbit][kBwdTileFast];
+#pragma unroll
+    for (int k = 0; k < kOrbit; ++k) cred[trow][k][lane] = acc[k];
+    __syncthreads();
+    if (grp == 0) {
+#pragma unroll
+      for (int k = 0; k < kOrbit; ++k) {
+        float t = cred[trow][k][lane];
+#pragma unroll
+        for (int q = 1; q < G; ++q) t += cred[trow + q * kRowsT][k][lane];
+        acc[k] = t;
+      }
+    }
+  }
+  double part = 0.0;
+  if (own && grp == 0) {
+#pragma unroll
+    for (int k = 0; k < kOrbit; ++k)
+      part += epi(ox[k], oy[k], 0, img_index<IO>(ox[k], oy[k], 0, d), acc[k]);
+  }
+  if (Epi::kReduce) {
+    const double t = block_sum(part, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
+  }
+}
+
 template <int SO, int IO, int SPLIT, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
 fan_fwd_quarter(const float* __restrict__ img, const float* __restrict__ ofs,

@@ -1,6 +1,7 @@
-"""Quarter-turn shared forward projection (float32 fan beam, single slices)
-against the oracle, the per-angle kernel, and through the fused solver
-epilogues."""
+"""Quarter-turn shared projections (float32 fan beam, single slices): the
+forward projection sharing a pixel's weights over the four angles of an
+orbit and the backprojection over pixel orbits, against the oracle, the
+per-angle kernels, and through the fused solver epilogues."""
 
 from __future__ import annotations
 
@@ -23,6 +24,10 @@ CFGS = {
                       detector_width=4.0, R=10.0, RE=5.0),
     "bench_like": dict(geometry="fanbeam", img_shape=(128, 128), angles=360, n_detectors=192,
                        detector_width=400.0, R=400.0, RE=200.0),
+    "two_pixels": dict(geometry="fanbeam", img_shape=(2, 2), angles=8, n_detectors=5,
+                       detector_width=6.0, R=10.0, RE=5.0),
+    "narrow_detector": dict(geometry="fanbeam", img_shape=(70, 70), angles=12, n_detectors=30,
+                            detector_width=30.0, R=200.0, RE=90.0),
 }
 
 
@@ -57,18 +62,64 @@ def test_quarter_forward(cuda_device, name, order):
     assert rel_l2(shared, direct) < 4e-6
 
 
-@pytest.mark.parametrize("name", ["plain", "shifted_detector"])
-def test_quarter_forward_in_solver_steps(cuda_device, name):
-    """Landweber and TV agree with the per-angle kernel to float32 rounding;
-    CG amplifies rounding, so it must be as close to the float64 oracle as
-    the per-angle kernel is."""
+def _backward(ps, sino_np, order, sym, split, cuda_device):
     import torch
 
     import gratopy_gb300 as gg
 
+    g = ps.gr_geometry(np.float32)
+    saved = (g.sym, g.bwd_split)
+    g.sym, g.bwd_split = sym, split
+    try:
+        s = gg.core.empty(ps.sinogram_shape, torch.float32, order, cuda_device)
+        s.copy_(torch.from_numpy(sino_np.astype(np.float32)))
+        return gg.backprojection(s, ps).double().cpu().numpy()
+    finally:
+        g.sym, g.bwd_split = saved
+
+
+@pytest.mark.parametrize("name", sorted(CFGS))
+@pytest.mark.parametrize("order", ["F", "C"])
+@pytest.mark.parametrize("split", [1, 2, 4, 8])
+def test_quarter_backprojection(cuda_device, name, order, split):
+    """Even sides run on pixel orbits with ``split`` angle groups, odd sides
+    keep the per-angle kernel; bins off the detector contribute nothing."""
+    ps = device_settings(CFGS[name], cuda_device)
+    sino = np.random.default_rng(3).random(ps.sinogram_shape)
+    ref = O.backward(np.asfortranarray(sino), host_settings(CFGS[name]))
+    shared = _backward(ps, sino, order, 4, split, cuda_device)
+    direct = _backward(ps, sino, order, 0, split, cuda_device)
+    assert rel_l2(shared, ref) < 1e-5
+    assert rel_l2(shared, direct) < 4e-6
+
+
+def test_quarter_backprojection_is_deterministic(cuda_device):
+    ps = device_settings(CFGS["bench_like"], cuda_device)
+    sino = np.random.default_rng(4).random(ps.sinogram_shape)
+    a = _backward(ps, sino, "F", 4, 4, cuda_device)
+    b = _backward(ps, sino, "F", 4, 4, cuda_device)
+    assert (a == b).all()
+
+
+@pytest.mark.parametrize("name", ["plain", "shifted_detector", "bench_like"])
+def test_quarter_projections_in_solver_steps(cuda_device, name):
+    """Landweber and TV agree with the per-angle kernels to float32 rounding;
+    CG amplifies rounding, so it is held to the float32 solver bound of the
+    parity tests: within max(1e-5, 3 x the float32 oracle's own distance
+    from the float64 oracle)."""
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300.phantom import random_ellipse_image
+
     ps = device_settings(CFGS[name], cuda_device)
     hps = host_settings(CFGS[name])
-    f_np = np.asfortranarray(np.random.default_rng(2).random(ps.sinogram_shape))
+    # a phantom's projection with 1% noise (a well-posed problem, as in the
+    # solver parity tests)
+    img = np.asfortranarray(random_ellipse_image(2, hps.img_shape[::-1]).T.astype(np.float64))
+    f_np = O.forward(img, hps)
+    f_np = np.asfortranarray(
+        f_np + 0.01 * np.abs(f_np).max() * np.random.default_rng(2).standard_normal(f_np.shape))
     f = gg.core.empty(ps.sinogram_shape, torch.float32, "F", cuda_device)
     f.copy_(torch.from_numpy(f_np.astype(np.float32)))
     g = ps.gr_geometry(np.float32)
@@ -79,9 +130,12 @@ def test_quarter_forward_in_solver_steps(cuda_device, name):
                     gg.landweber(f, ps, 5, norm_estimate=5.0).double().cpu().numpy(),
                     gg.total_variation(f, ps, 10.0, 5, norm_estimate=5.0).double().cpu().numpy())
     g.sym = 4
-    cg_ref = O.conjugate_gradients(np.asfortranarray(f_np.astype(np.float32).astype(np.float64)),
-                                   hps, 5)
-    assert rel_l2(res[4][0], cg_ref) <= 2 * rel_l2(res[0][0], cg_ref) + 1e-6
+    f32 = np.asfortranarray(f_np.astype(np.float32))
+    cg_ref = O.conjugate_gradients(f32.astype(np.float64), hps, 5)
+    base = rel_l2(O.conjugate_gradients(f32, hps, 5), cg_ref)
+    for sym in (4, 0):
+        err = rel_l2(res[sym][0], cg_ref)
+        assert err <= max(1e-5, 3 * base), f"sym {sym}: CG rel err {err:.3e}, float32 oracle {base:.3e}"
     for a, b in zip(res[4][1:], res[0][1:]):
         assert rel_l2(a, b) < 1e-5
 
