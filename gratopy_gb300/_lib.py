@@ -37,6 +37,8 @@ class GrGeometry(ctypes.Structure):
         ("bwd_split", ctypes.c_int),
         ("sym", ctypes.c_int),
         ("sym_map", (ctypes.c_int * 6) * 3),
+        ("work", ctypes.c_void_p),
+        ("work_bytes", ctypes.c_size_t),
     ]
 
 
@@ -103,6 +105,8 @@ SIGNATURES = {
     "gr_batch_sino_step": (_I, [_P, _P, _I, _I, _I, _P]),
     "gr_batch_scalars": (_I, [_P, _P, _I, _I, _I, _P]),
     "gr_forward_partials": (_Z, [_G, _I]),
+    "gr_work_bytes": (_Z, [_G, _I]),
+    "gr_geometry_size": (_Z, []),
     "gr_backward_partials": (_Z, [_G, _I, _I]),
     "gr_weight_sinogram": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "gr_equ_mul_add": (_I, [_P, _D, _P, _I, _Z, _P]),

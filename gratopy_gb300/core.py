@@ -191,6 +191,8 @@ class ProjectionSettings:
         self._dev = {}
         self._geom = {}
         self._geom_adj = {}
+        self._work_bytes = {}  # scratch bytes the projections can use, per precision
+        self._work = {}  # (precision, stream) -> scratch tensor
 
         if self.reverse_detector and self.is_parallel:
             print(
@@ -333,6 +335,7 @@ class ProjectionSettings:
         ga = _lib.GrGeometry.from_buffer_copy(g)
         ga.ofs = tables["ofs_adj"].data_ptr()
         self._geom_adj[dtype] = ga
+        self._work_bytes[dtype] = int(_lib.raw("gr_work_bytes")(ctypes.byref(g), 1))
 
     def quarter_maps(self):
         """Index maps of a quarter-turn symmetric fan-beam geometry (see
@@ -363,14 +366,40 @@ class ProjectionSettings:
         return self._dev[_np_dtype(dtype)]
 
     def gr_geometry(self, dtype) -> _lib.GrGeometry:
-        """C-ABI geometry descriptor for precision ``dtype`` (tables uploaded)."""
+        """C-ABI geometry descriptor for precision ``dtype`` (tables uploaded).
+
+        The descriptor carries the scratch of the current stream (see
+        :meth:`_bind_work`); a descriptor kept across calls on several
+        streams at once must be fetched again on each stream.
+        """
         self.ensure_dtype(dtype)
-        return self._geom[_np_dtype(dtype)]
+        dt = _np_dtype(dtype)
+        return self._bind_work(self._geom[dt], dt)
 
     def gr_geometry_adjoint(self, dtype) -> _lib.GrGeometry:
         """Descriptor whose backprojection is the plain transpose of the forward projection."""
         self.ensure_dtype(dtype)
-        return self._geom_adj[_np_dtype(dtype)]
+        dt = _np_dtype(dtype)
+        return self._bind_work(self._geom_adj[dt], dt)
+
+    def _bind_work(self, g, dt):
+        """Point ``g.work`` at this settings object's scratch for the current
+        stream (allocated on first use; the library uses it stream-ordered).
+        During a stream capture the descriptor keeps the scratch bound before
+        the capture, the one of the stream that replays the graph."""
+        nbytes = self._work_bytes.get(dt, 0)
+        if not nbytes or torch.cuda.is_current_stream_capturing():
+            return g
+        stream = torch.cuda.current_stream(self.device)
+        key = (dt, stream.cuda_stream)
+        buf = self._work.get(key)
+        if buf is None:
+            with torch.cuda.device(self.device):
+                buf = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            self._work[key] = buf
+        g.work = buf.data_ptr()
+        g.work_bytes = nbytes
+        return g
 
     def set_angle_weights(self, angle_weights) -> None:
         """Replace the angle weights and re-upload the tables (gratopy.py:1697-1756)."""

@@ -64,6 +64,13 @@ int gr_fan_bwd(void* img, const void* sino, const void* ofs, const void* sdpd, c
   return gr_backward(&g, img, sino, Nz, img_order, sino_order, stream);
 }
 
+size_t gr_work_bytes(const gr_geometry* g, int Nz) {
+  if (Nz <= 0 || launch::check_geometry(g) != GR_OK) return 0;
+  return launch::orbit_work_bytes(g, Nz);
+}
+
+size_t gr_geometry_size(void) { return sizeof(gr_geometry); }
+
 size_t gr_forward_partials(const gr_geometry* g, int Nz) {
   if (g == nullptr || Nz <= 0) return 0;
   const dim3 grid = launch::fwd_grid(g, Nz, launch::fwd_split(g, Nz));

@@ -178,6 +178,12 @@ inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
   return true;
 }
 
+// Scratch of the orbit backprojection: the interleaved rows (one float4 per
+// base angle and bin).
+inline size_t orbit_work_bytes(const gr_geometry* g, int Nz) {
+  return use_quarter_bwd(g, Nz) ? (size_t)(g->Na / 4) * (size_t)g->Ns * sizeof(float4) : 0;
+}
+
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   const int ZB = zblock(Nz);
   const int group = g->dtype == GR_F32 ? fast::kRayGroup : 1;  // bins per lane group
@@ -285,9 +291,22 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
     constexpr int PY = (SPLIT == 1 && ZB == 1) ? 2 : 1;
     const dim3 fblock(kBwdTileFast, kBwdTileSlow / PY);
     if (ZB == 1 && use_quarter_bwd(g, Nz)) {
-      fast::fan_bwd_orbit<IO, SO, SPLIT, Epi><<<grid, block, 0, st>>>(
-          sino, static_cast<const float*>(g->ofs), static_cast<const float*>(g->sdpd),
-          fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials, skip);
+      const float* ofs = static_cast<const float*>(g->ofs);
+      const float* sdpd = static_cast<const float*>(g->sdpd);
+      const size_t need = orbit_work_bytes(g, Nz);
+      if (g->work != nullptr && g->work_bytes >= need &&
+          (reinterpret_cast<uintptr_t>(g->work) & 15u) == 0) {
+        float4* rows4 = static_cast<float4*>(g->work);
+        const dim3 rgrid((g->Ns + 255) / 256, g->Na / 4);
+        fast::orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, sdpd, d, rows4, skip);
+        fast::fan_bwd_orbit<IO, SO, SPLIT, true, Epi><<<grid, block, 0, st>>>(
+            sino, rows4, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials,
+            skip);
+      } else {
+        fast::fan_bwd_orbit<IO, SO, SPLIT, false, Epi><<<grid, block, 0, st>>>(
+            sino, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials,
+            skip);
+      }
     } else if (g->kind == GR_RADON) {
       fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, fblock, 0, st>>>(
           sino, static_cast<const float*>(g->ofs), d, epi, partials, skip);
@@ -348,6 +367,8 @@ inline gr_geometry make_geo(int kind, int dtype, const void* ofs, const void* sd
   g.sym = 0;  // the reference-style entries keep every angle's own geometry
   for (int m = 0; m < 3; ++m)
     for (int k = 0; k < 6; ++k) g.sym_map[m][k] = 0;
+  g.work = nullptr;
+  g.work_bytes = 0;
   g.ofs = ofs;
   g.sdpd = sdpd;
   const int n = kind == GR_RADON ? 6 : 11;

@@ -919,6 +919,27 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
   return part;
 }
 
+// The four sinogram rows of every quarter-turn orbit of angles, premultiplied
+// by sdpd, as one float4 per (base angle, bin): rows4[a Ns + s] =
+// sdpd[s] (sino[s, a], sino[s, a + Q], sino[s, a + 2Q], sino[s, a + 3Q]),
+// Q = Na / 4.  Lanes run along the bins (coalesced for F-ordered sinograms).
+template <int SO>
+__global__ void __launch_bounds__(256)
+orbit_rows(const float* __restrict__ sino, const float* __restrict__ sdpd, Dims d,
+           float4* __restrict__ rows4, const int* __restrict__ skip) {
+  if (skip != nullptr && *skip) return;
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t a = blockIdx.y;
+  if (s >= d.Ns) return;
+  int64_t ss_, sa_, sz_;
+  sino_strides<SO>(d, ss_, sa_, sz_);
+  const int64_t Q = d.Na / 4;
+  const float* p = sino + s * ss_ + a * sa_;
+  const float w = ldg(sdpd + s);
+  rows4[a * d.Ns + s] = make_float4(w * ldg(p), w * ldg(p + Q * sa_), w * ldg(p + 2 * Q * sa_),
+                                    w * ldg(p + 3 * Q * sa_));
+}
+
 // Backprojection over quarter-turn pixel orbits.  With the maps powers of
 // one quarter turn A (A_m = A^m about the image centre, N even) the pixels
 // P_k = A^k P_0 satisfy u(a + j Na/4, P_k) = u(a, P_{k-j mod 4}) for the
@@ -928,13 +949,16 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
 // each to the four sinogram rows a + j Na/4, i.e. one reciprocal, one floor
 // and two sdpd loads serve four pixel-angles.  The sinogram values are read
 // directly (the rows of the four angles are L1/L2 resident; no staging, no
-// barrier in the angle loop).  The G thread groups of a block take
-// interleaved base angles and are added in a fixed order at the end.
-template <int IO, int SO, int G, class Epi>
+// barrier in the angle loop); with ROWS4 they come from the interleaved copy
+// made by orbit_rows, two float4 loads per pixel and base angle instead of
+// ten scalar loads.  The G thread groups of a block take interleaved base
+// angles and are added in a fixed order at the end.
+template <int IO, int SO, int G, bool ROWS4, class Epi>
 __global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
-fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
-              const float* __restrict__ sdpd, FanGeo<float> gg, Dims d, QuarterMaps qm,
-              Epi epi, double* __restrict__ partials, const int* __restrict__ skip) {
+fan_bwd_orbit(const float* __restrict__ sino, const float4* __restrict__ rows4,
+              const float* __restrict__ ofs, const float* __restrict__ sdpd, FanGeo<float> gg,
+              Dims d, QuarterMaps qm, Epi epi, double* __restrict__ partials,
+              const int* __restrict__ skip) {
   constexpr int kOrbit = 4;
   constexpr int kRowsT = kBwdTileSlow / G;  // quadrant rows of the block tile
   __shared__ double red[32];
@@ -1008,12 +1032,27 @@ fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
       const bool okm = (unsigned)xm < (unsigned)Ns;
       const bool okp = (unsigned)(xm + 1) < (unsigned)Ns;
       const int im = okm ? xm : 0, ip = okp ? xm + 1 : 0;
-      const float Wm = okm ? (1.0f - fr) * inv * ldg(sdpd + im) : 0.0f;
-      const float Wp = okp ? fr * inv * ldg(sdpd + ip) : 0.0f;
+      if constexpr (ROWS4) {
+        // the four rows of the orbit, premultiplied by sdpd, in one load
+        const float Wm = okm ? (1.0f - fr) * inv : 0.0f;
+        const float Wp = okp ? fr * inv : 0.0f;
+        const float4 v0 = __ldg(rows4 + (int64_t)a * Ns + im);
+        const float4 v1 = __ldg(rows4 + (int64_t)a * Ns + ip);
+        const float vm[kOrbit] = {v0.x, v0.y, v0.z, v0.w};
+        const float vp[kOrbit] = {v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
-      for (int j = 0; j < kOrbit; ++j) {
-        const float v = fmaf(Wp, ldg(row[j] + ip * ss), Wm * ldg(row[j] + im * ss));
-        acc[(i + j) % kOrbit] = fmaf(wj[j], v, acc[(i + j) % kOrbit]);
+        for (int j = 0; j < kOrbit; ++j) {
+          const float v = fmaf(Wp, vp[j], Wm * vm[j]);
+          acc[(i + j) % kOrbit] = fmaf(wj[j], v, acc[(i + j) % kOrbit]);
+        }
+      } else {
+        const float Wm = okm ? (1.0f - fr) * inv * ldg(sdpd + im) : 0.0f;
+        const float Wp = okp ? fr * inv * ldg(sdpd + ip) : 0.0f;
+#pragma unroll
+        for (int j = 0; j < kOrbit; ++j) {
+          const float v = fmaf(Wp, ldg(row[j] + ip * ss), Wm * ldg(row[j] + im * ss));
+          acc[(i + j) % kOrbit] = fmaf(wj[j], v, acc[(i + j) % kOrbit]);
+        }
       }
     }
   }

@@ -70,9 +70,22 @@ typedef struct gr_geometry {
    * four angles.  Set by the Python layer after checking the geometry. */
   int sym;
   int sym_map[3][6];
+  /* Device scratch (no counterpart in the reference) that a call may use
+   * while it runs, stream-ordered: the fan-beam backprojection over
+   * quarter-turn orbits keeps an interleaved copy of the four sinogram rows
+   * of every angle orbit there (gr_work_bytes gives the size).  NULL or
+   * smaller than that: the kernels read the sinogram directly.  Calls that
+   * may run at the same time must not share it. */
+  void* work;
+  size_t work_bytes;
 } gr_geometry;
 
 GR_API const char* gr_error_string(int code);
+/* Scratch bytes the projections of g on Nz slices can use (gr_geometry.work);
+ * 0 when they use none. */
+GR_API size_t gr_work_bytes(const gr_geometry* g, int Nz);
+/* sizeof(gr_geometry), for bindings that mirror the struct. */
+GR_API size_t gr_geometry_size(void);
 /* Last CUDA error seen by this library on the calling thread (cudaError_t). */
 GR_API int gr_last_cuda_error(void);
 GR_API int gr_version(void);

@@ -70,11 +70,15 @@ def test_host_only_entry_points(library):
     q.ofs, q.sdpd = fake, fake
     turn = [(0, -1, 1, 0, 7, 0), (-1, 0, 0, -1, 7, 7), (0, 1, -1, 0, 0, 7)]
 
-    def forward_rc(sym, maps):
+    def set_maps(sym, maps):
         q.sym = sym
         for m, row in enumerate(maps):
             for k, v in enumerate(row):
                 q.sym_map[m][k] = v
+
+    def forward_rc(sym, maps):
+        assert q.Na > 65535  # never a launch: every case is rejected
+        set_maps(sym, maps)
         return lib.gr_forward(ctypes.byref(q), fake, fake, 1, 0, 0, None)
 
     assert forward_rc(4, turn) == 4
@@ -84,8 +88,23 @@ def test_host_only_entry_points(library):
     assert forward_rc(4, [turn[0], (1, 1, 0, -1, 0, 7), turn[2]]) == 1  # not a permutation
     q.Ny = 9
     assert forward_rc(4, turn) == 1  # not square
+    # scratch of the orbit backprojection: one float4 per base angle and bin,
+    # only for float32 single slices of an even side with cyclic maps
+    q.Ny, q.Na = 8, 8
+    set_maps(4, turn)
+    work = lib.gr_work_bytes
+    assert work(ctypes.byref(q), 1) == (8 // 4) * 4 * 16
+    assert work(ctypes.byref(q), 3) == 0
+    q.dtype = 1
+    assert work(ctypes.byref(q), 1) == 0
+    q.dtype = 0
+    set_maps(4, [turn[1], turn[0], turn[2]])  # valid maps, not powers of one turn
+    assert work(ctypes.byref(q), 1) == 0
+    set_maps(0, turn)
+    assert work(ctypes.byref(q), 1) == 0
     assert lib.gr_forward_partials(None, 1) == 0
-    # batched descriptors: binding layout equals the library's
+    # descriptors: binding layouts equal the library's
+    assert lib.gr_geometry_size() == ctypes.sizeof(_lib.GrGeometry)
     assert lib.gr_batch_problem_size() == ctypes.sizeof(_lib.GrBatchProblem)
     assert lib.gr_batch_forward(None, None, 1, 0, 1, None) == 1
     assert lib.gr_batch_scalars(None, None, 1, 0, 1, None) == 1

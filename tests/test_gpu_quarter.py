@@ -93,6 +93,66 @@ def test_quarter_backprojection(cuda_device, name, order, split):
     assert rel_l2(shared, direct) < 4e-6
 
 
+def _backward_raw(ps, sino_np, work, work_bytes, cuda_device):
+    """Backprojection through gr_backward with the given scratch."""
+    import ctypes
+
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import _lib, core
+
+    g = _lib.GrGeometry.from_buffer_copy(ps.gr_geometry(np.float32))
+    g.work, g.work_bytes = work, work_bytes
+    s = gg.core.empty(ps.sinogram_shape, torch.float32, "F", cuda_device)
+    s.copy_(torch.from_numpy(sino_np.astype(np.float32)))
+    out = gg.core.empty(ps.img_shape, torch.float32, "F", cuda_device)
+    _lib.call("gr_backward", ctypes.byref(g), core._ptr(out), core._ptr(s), 1, 0, 0,
+              core._stream_ptr(cuda_device))
+    return out.double().cpu().numpy()
+
+
+@pytest.mark.parametrize("name", ["plain", "narrow_detector", "two_pixels"])
+def test_orbit_scratch_and_direct_gather_agree(cuda_device, name):
+    """With the interleaved-row scratch, without it, and with one too small
+    (the kernels then read the sinogram directly)."""
+    import ctypes
+
+    from gratopy_gb300 import _lib
+
+    ps = device_settings(CFGS[name], cuda_device)
+    g = ps.gr_geometry(np.float32)
+    need = int(_lib.raw("gr_work_bytes")(ctypes.byref(g), 1))
+    assert need == (ps.n_angles // 4) * ps.sinogram_shape[0] * 16
+    assert g.work and g.work_bytes == need
+    sino = np.random.default_rng(6).random(ps.sinogram_shape)
+    ref = O.backward(np.asfortranarray(sino), host_settings(CFGS[name]))
+    with_rows = _backward_raw(ps, sino, g.work, need, cuda_device)
+    direct = _backward_raw(ps, sino, None, 0, cuda_device)
+    small = _backward_raw(ps, sino, g.work, need - 16, cuda_device)
+    assert rel_l2(with_rows, ref) < 1e-5 and rel_l2(direct, ref) < 1e-5
+    assert rel_l2(with_rows, direct) < 1e-6
+    assert (small == direct).all()
+
+
+def test_orbit_scratch_per_stream(cuda_device):
+    import torch
+
+    import gratopy_gb300 as gg
+
+    ps = device_settings(CFGS["bench_like"], cuda_device)
+    sino = torch.rand(ps.sinogram_shape, device=cuda_device).T.contiguous().T
+    a = gg.backprojection(sino, ps)
+    side = torch.cuda.Stream(cuda_device)
+    side.wait_stream(torch.cuda.current_stream(cuda_device))
+    with torch.cuda.stream(side):
+        b = gg.backprojection(sino, ps)
+    torch.cuda.current_stream(cuda_device).wait_stream(side)
+    keys = [k for k in ps._work if k[0] == np.dtype(np.float32)]
+    assert len(keys) == 2 and keys[0][1] != keys[1][1]
+    assert torch.equal(a, b)
+
+
 def test_quarter_backprojection_is_deterministic(cuda_device):
     ps = device_settings(CFGS["bench_like"], cuda_device)
     sino = np.random.default_rng(4).random(ps.sinogram_shape)
