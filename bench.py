@@ -496,15 +496,14 @@ DEFAULT_EXTRAS = [e for e in EXTRAS if e != "large_stack_c"]
 
 
 def launches_per_step(ps):
-    """Kernels of one forward + backprojection: the orbit backprojection with
-    its scratch first interleaves the sinogram rows (one more launch)."""
-    import ctypes
-
-    from gratopy_gb300 import _lib
-
+    """Kernels of one forward + backprojection.  With quarter-turn maps and
+    scratch bound, the forward first gathers each pixel's orbit into one
+    float4 and the orbit backprojection (even sides) first interleaves the
+    sinogram rows: one more launch each."""
     g = ps.gr_geometry(np.float32)
-    rows = int(_lib.raw("gr_work_bytes")(ctypes.byref(g), 1)) > 0 and bool(g.work)
-    return 3 if rows else 2
+    if g.sym != 4 or not g.work:
+        return 2
+    return 4 if ps.img_shape[0] % 2 == 0 else 3
 
 
 def cpu_baseline_sample(max_seconds=12.0):

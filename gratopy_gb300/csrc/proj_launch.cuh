@@ -178,10 +178,39 @@ inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
   return true;
 }
 
-// Scratch of the orbit backprojection: the interleaved rows (one float4 per
-// base angle and bin).
+// Scratch of the orbit kernels: the forward's orbit pixels (one float4 per
+// pixel) and the backprojection's interleaved rows (one float4 per base
+// angle and bin); one call uses one of them, so the larger one is needed.
+// Below these sizes (pixel-angles per projection) the extra launch costs more
+// than the copy saves (measured: the forward's copy loses at 256^2 x 360 and
+// wins at 512^2 x 360, the backprojection's loses at 128^2 x 360 and wins at
+// 256^2 x 360).
+constexpr int64_t kQuarterFwdCopyMin = 48ll << 20;
+constexpr int64_t kQuarterBwdCopyMin = 12ll << 20;
+
+inline int64_t pixel_angles(const gr_geometry* g) {
+  return (int64_t)g->Nx * g->Ny * g->Na;
+}
+
+inline size_t quarter_fwd_bytes(const gr_geometry* g, int Nz) {
+  if (!use_quarter(g, Nz) || pixel_angles(g) < kQuarterFwdCopyMin) return 0;
+  return (size_t)g->Nx * (size_t)g->Ny * sizeof(float4);
+}
+
+inline size_t quarter_bwd_bytes(const gr_geometry* g, int Nz) {
+  if (!use_quarter_bwd(g, Nz) || pixel_angles(g) < kQuarterBwdCopyMin) return 0;
+  return (size_t)(g->Na / 4) * (size_t)g->Ns * sizeof(float4);
+}
+
 inline size_t orbit_work_bytes(const gr_geometry* g, int Nz) {
-  return use_quarter_bwd(g, Nz) ? (size_t)(g->Na / 4) * (size_t)g->Ns * sizeof(float4) : 0;
+  const size_t f = quarter_fwd_bytes(g, Nz), b = quarter_bwd_bytes(g, Nz);
+  return f > b ? f : b;
+}
+
+// The caller's scratch holds `need` bytes on a 16-byte boundary.
+inline bool work_fits(const gr_geometry* g, size_t need) {
+  return need > 0 && g->work != nullptr && g->work_bytes >= need &&
+         (reinterpret_cast<uintptr_t>(g->work) & 15u) == 0;
 }
 
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
@@ -228,9 +257,19 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
       fast::radon_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
           img, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi, partials, skip);
     } else if (ZB == 1 && use_quarter(g, Nz)) {
-      fast::fan_fwd_quarter<SO, IO, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
-          img, static_cast<const float*>(g->ofs), static_cast<const float*>(g->sdpd),
-          fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials, skip);
+      const float* ofs = static_cast<const float*>(g->ofs);
+      const float* sdpd = static_cast<const float*>(g->sdpd);
+      const fast::QuarterMaps qm = quarter_maps(g);
+      if (work_fits(g, quarter_fwd_bytes(g, Nz))) {
+        float4* img4 = static_cast<float4*>(g->work);
+        const dim3 pgrid((g->Nx + 255) / 256, g->Ny);
+        fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, skip);
+        fast::fan_fwd_quarter<SO, IO, SPLIT, true, Epi><<<grid, kFwdBlock, 0, st>>>(
+            img, img4, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi, partials, skip);
+      } else {
+        fast::fan_fwd_quarter<SO, IO, SPLIT, false, Epi><<<grid, kFwdBlock, 0, st>>>(
+            img, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi, partials, skip);
+      }
     } else {
       fast::fan_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
           img, static_cast<const float*>(g->ofs), static_cast<const float*>(g->sdpd),
@@ -293,9 +332,7 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
     if (ZB == 1 && use_quarter_bwd(g, Nz)) {
       const float* ofs = static_cast<const float*>(g->ofs);
       const float* sdpd = static_cast<const float*>(g->sdpd);
-      const size_t need = orbit_work_bytes(g, Nz);
-      if (g->work != nullptr && g->work_bytes >= need &&
-          (reinterpret_cast<uintptr_t>(g->work) & 15u) == 0) {
+      if (work_fits(g, quarter_bwd_bytes(g, Nz))) {
         float4* rows4 = static_cast<float4*>(g->work);
         const dim3 rgrid((g->Ns + 255) / 256, g->Na / 4);
         fast::orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, sdpd, d, rows4, skip);

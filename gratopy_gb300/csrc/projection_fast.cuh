@@ -781,8 +781,9 @@ struct QuarterMaps {
   int axx[3], axy[3], ayx[3], ayy[3], cx[3], cy[3];
 };
 
-template <int SO, int IO, int SPLIT, class Epi>
+template <int SO, int IO, int SPLIT, bool PIX4, class Epi>
 __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__ img,
+                                                       const float4* __restrict__ img4,
                                                        const float* __restrict__ ofs,
                                                        const float* __restrict__ sdpd,
                                                        FanGeo<float> g, Dims d, QuarterMaps qm,
@@ -817,6 +818,10 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
     int Nyy = (int)d.Ny, Nxx = (int)d.Nx;
     int64_t sx, sy, sz;
     img_strides<IO>(d, sx, sy, sz);
+    if constexpr (PIX4) {  // the orbit copy is x-fastest whatever the image order
+      sx = 1;
+      sy = d.Nx;
+    }
     // element steps of the turned pixels along the array's x and y axes
     // (32-bit: a single slice of at most 2^31 pixels)
     int mstep_x[kOrbit - 1], mstep_y[kOrbit - 1], mbase[kOrbit - 1];
@@ -872,15 +877,25 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
       const int stp = (int)step_x;
       int o0 = (int)(y * step_y + xlo * step_x);
       int om[kOrbit - 1];
+      if constexpr (!PIX4) {
 #pragma unroll
-      for (int m = 0; m < kOrbit - 1; ++m) om[m] = mbase[m] + y * mstep_y[m] + xlo * mstep_x[m];
+        for (int m = 0; m < kOrbit - 1; ++m) om[m] = mbase[m] + y * mstep_y[m] + xlo * mstep_x[m];
+      }
       for (int x = xlo; x <= xhi; ++x) {
         const float r = rcp_approx(t);
         const float u = fmaf(ss, r, -s_mid0);
         float v[kOrbit];
-        v[0] = ldg(img + o0) * r;
+        if constexpr (PIX4) {
+          const float4 p4 = __ldg(img4 + o0);
+          v[0] = p4.x * r;
+          v[1] = p4.y * r;
+          v[2] = p4.z * r;
+          v[3] = p4.w * r;
+        } else {
+          v[0] = ldg(img + o0) * r;
 #pragma unroll
-        for (int m = 0; m < kOrbit - 1; ++m) v[m + 1] = ldg(img + om[m]) * r;
+          for (int m = 0; m < kOrbit - 1; ++m) v[m + 1] = ldg(img + om[m]) * r;
+        }
 #pragma unroll
         for (int q = 0; q < kRayGroup; ++q) {
           const float w = 1.0f - fabsf((float)q - u);
@@ -890,8 +905,10 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
           }
         }
         o0 += stp;
+        if constexpr (!PIX4) {
 #pragma unroll
-        for (int m = 0; m < kOrbit - 1; ++m) om[m] += mstep_x[m];
+          for (int m = 0; m < kOrbit - 1; ++m) om[m] += mstep_x[m];
+        }
         t += ddx;
         ss += dx;
       }
@@ -917,6 +934,28 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
     }
   }
   return part;
+}
+
+// The four pixels a candidate of the orbit-sharing forward projection loads,
+// as one float4 per pixel: img4[x + Nx y] = (img(P), img(M_1 P), img(M_2 P),
+// img(M_3 P)) for P = (x, y) and the quarter-turn index maps M_m.
+template <int IO>
+__global__ void __launch_bounds__(256)
+orbit_pixels(const float* __restrict__ img, Dims d, QuarterMaps qm, float4* __restrict__ img4,
+             const int* __restrict__ skip) {
+  if (skip != nullptr && *skip) return;
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t y = blockIdx.y;
+  if (x >= d.Nx) return;
+  float v[4];
+  v[0] = ldg(img + img_index<IO>(x, y, 0, d));
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const int64_t mx = qm.cx[m] + qm.axx[m] * x + qm.axy[m] * y;
+    const int64_t my = qm.cy[m] + qm.ayx[m] * x + qm.ayy[m] * y;
+    v[m + 1] = ldg(img + img_index<IO>(mx, my, 0, d));
+  }
+  img4[x + d.Nx * y] = make_float4(v[0], v[1], v[2], v[3]);
 }
 
 // The four sinogram rows of every quarter-turn orbit of angles, premultiplied
@@ -1084,15 +1123,17 @@ fan_bwd_orbit(const float* __restrict__ sino, const float4* __restrict__ rows4,
   }
 }
 
-template <int SO, int IO, int SPLIT, class Epi>
+template <int SO, int IO, int SPLIT, bool PIX4, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
-fan_fwd_quarter(const float* __restrict__ img, const float* __restrict__ ofs,
+fan_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4,
+                const float* __restrict__ ofs,
                 const float* __restrict__ sdpd, FanGeo<float> g, Dims d, QuarterMaps qm, Epi epi,
                 double* __restrict__ partials, const int* __restrict__ skip) {
   __shared__ double red[32];
   if (skip != nullptr && *skip) return;
   const double part =
-      fan_fwd_quarter_tile<SO, IO, SPLIT, Epi>(img, ofs, sdpd, g, d, qm, epi, blockIdx);
+      fan_fwd_quarter_tile<SO, IO, SPLIT, PIX4, Epi>(img, img4, ofs, sdpd, g, d, qm, epi,
+                                                     blockIdx);
   if (Epi::kReduce) {
     double t = block_sum(part, red);
     if (threadIdx.x + blockDim.x * threadIdx.y == 0)

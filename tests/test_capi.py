@@ -88,19 +88,32 @@ def test_host_only_entry_points(library):
     assert forward_rc(4, [turn[0], (1, 1, 0, -1, 0, 7), turn[2]]) == 1  # not a permutation
     q.Ny = 9
     assert forward_rc(4, turn) == 1  # not square
-    # scratch of the orbit backprojection: one float4 per base angle and bin,
-    # only for float32 single slices of an even side with cyclic maps
-    q.Ny, q.Na = 8, 8
-    set_maps(4, turn)
+    # scratch of the orbit kernels (float32 single slices): the forward's
+    # float4 per pixel (from 48 Mi pixel-angles per projection), the
+    # backprojection's float4 per base angle and bin (even sides with cyclic
+    # maps, from 12 Mi pixel-angles); the larger of the two
     work = lib.gr_work_bytes
-    assert work(ctypes.byref(q), 1) == (8 // 4) * 4 * 16
+
+    def sized(N, Ns, Na, maps=None):
+        q.Nx = q.Ny = N
+        q.Ns, q.Na = Ns, Na
+        c = N - 1
+        set_maps(4, maps or [(0, -1, 1, 0, c, 0), (-1, 0, 0, -1, c, c), (0, 1, -1, 0, 0, c)])
+        return work(ctypes.byref(q), 1)
+
+    assert sized(512, 768, 360) == max(512 * 512 * 16, 90 * 768 * 16)
+    assert sized(512, 4000, 400) == 100 * 4000 * 16
+    assert sized(256, 384, 360) == 90 * 384 * 16  # the backprojection's only
+    assert sized(128, 192, 360) == 0
+    sized(512, 768, 360)
     assert work(ctypes.byref(q), 3) == 0
     q.dtype = 1
     assert work(ctypes.byref(q), 1) == 0
     q.dtype = 0
-    set_maps(4, [turn[1], turn[0], turn[2]])  # valid maps, not powers of one turn
-    assert work(ctypes.byref(q), 1) == 0
-    set_maps(0, turn)
+    c = 511  # valid maps, not the powers of one quarter turn: the forward's only
+    assert sized(512, 768, 360, [(-1, 0, 0, -1, c, c), (0, -1, 1, 0, c, 0),
+                                 (0, 1, -1, 0, 0, c)]) == 512 * 512 * 16
+    set_maps(0, [(0,) * 6] * 3)
     assert work(ctypes.byref(q), 1) == 0
     assert lib.gr_forward_partials(None, 1) == 0
     # descriptors: binding layouts equal the library's

@@ -93,8 +93,8 @@ def test_quarter_backprojection(cuda_device, name, order, split):
     assert rel_l2(shared, direct) < 4e-6
 
 
-def _backward_raw(ps, sino_np, work, work_bytes, cuda_device):
-    """Backprojection through gr_backward with the given scratch."""
+def _raw(ps, fwd, data_np, work, work_bytes, cuda_device):
+    """One projection through gr_forward / gr_backward with the given scratch."""
     import ctypes
 
     import torch
@@ -104,35 +104,69 @@ def _backward_raw(ps, sino_np, work, work_bytes, cuda_device):
 
     g = _lib.GrGeometry.from_buffer_copy(ps.gr_geometry(np.float32))
     g.work, g.work_bytes = work, work_bytes
-    s = gg.core.empty(ps.sinogram_shape, torch.float32, "F", cuda_device)
-    s.copy_(torch.from_numpy(sino_np.astype(np.float32)))
-    out = gg.core.empty(ps.img_shape, torch.float32, "F", cuda_device)
-    _lib.call("gr_backward", ctypes.byref(g), core._ptr(out), core._ptr(s), 1, 0, 0,
-              core._stream_ptr(cuda_device))
+    in_shape, out_shape = ((ps.img_shape, ps.sinogram_shape) if fwd
+                           else (ps.sinogram_shape, ps.img_shape))
+    x = gg.core.empty(in_shape, torch.float32, "F", cuda_device)
+    x.copy_(torch.from_numpy(data_np.astype(np.float32)))
+    out = gg.core.empty(out_shape, torch.float32, "F", cuda_device)
+    _lib.call("gr_forward" if fwd else "gr_backward", ctypes.byref(g), core._ptr(out),
+              core._ptr(x), 1, 0, 0, core._stream_ptr(cuda_device))
     return out.double().cpu().numpy()
 
 
-@pytest.mark.parametrize("name", ["plain", "narrow_detector", "two_pixels"])
-def test_orbit_scratch_and_direct_gather_agree(cuda_device, name):
-    """With the interleaved-row scratch, without it, and with one too small
-    (the kernels then read the sinogram directly)."""
+# sizes at which the orbit kernels work from interleaved scratch copies
+# (48 * 2^20 pixel-angles for the forward, 12 * 2^20 for the backprojection)
+COPY_CFGS = {
+    "copy_even": dict(geometry="fanbeam", img_shape=(360, 360), angles=480, n_detectors=540,
+                      detector_width=400.0, R=400.0, RE=200.0),
+    "copy_odd": dict(geometry="fanbeam", img_shape=(361, 361), angles=480, n_detectors=530,
+                     detector_width=400.0, R=400.0, RE=200.0, detector_shift=3.0),
+}
+
+
+def test_small_problems_bind_no_scratch(cuda_device):
+    for name in ("plain", "bench_like", "two_pixels"):
+        ps = device_settings(CFGS[name], cuda_device)
+        g = ps.gr_geometry(np.float32)
+        assert g.sym == 4 and not g.work and g.work_bytes == 0
+
+
+@pytest.mark.parametrize("name", sorted(COPY_CFGS))
+@pytest.mark.parametrize("fwd", [True, False])
+def test_orbit_scratch_and_direct_gather_agree(cuda_device, name, fwd):
+    """With the interleaved scratch copy, without scratch, and with scratch
+    one float4 too small (the kernels then read their input directly)."""
     import ctypes
 
     from gratopy_gb300 import _lib
 
-    ps = device_settings(CFGS[name], cuda_device)
+    cfg = COPY_CFGS[name]
+    ps = device_settings(cfg, cuda_device)
+    hps = host_settings(cfg)
     g = ps.gr_geometry(np.float32)
+    Nx, Ny = ps.img_shape
+    Ns, Na = ps.sinogram_shape
+    fwd_need = Nx * Ny * 16
+    bwd_need = (Na // 4) * Ns * 16 if Nx % 2 == 0 else 0
     need = int(_lib.raw("gr_work_bytes")(ctypes.byref(g), 1))
-    assert need == (ps.n_angles // 4) * ps.sinogram_shape[0] * 16
-    assert g.work and g.work_bytes == need
-    sino = np.random.default_rng(6).random(ps.sinogram_shape)
-    ref = O.backward(np.asfortranarray(sino), host_settings(CFGS[name]))
-    with_rows = _backward_raw(ps, sino, g.work, need, cuda_device)
-    direct = _backward_raw(ps, sino, None, 0, cuda_device)
-    small = _backward_raw(ps, sino, g.work, need - 16, cuda_device)
-    assert rel_l2(with_rows, ref) < 1e-5 and rel_l2(direct, ref) < 1e-5
-    assert rel_l2(with_rows, direct) < 1e-6
-    assert (small == direct).all()
+    assert need == max(fwd_need, bwd_need)
+    assert g.sym == 4 and g.work and g.work_bytes == need
+    rng = np.random.default_rng(6)
+    if fwd:
+        data = rng.random(ps.img_shape)
+        ref = O.forward(np.asfortranarray(data), hps)
+        own = fwd_need
+    else:
+        data = rng.random(ps.sinogram_shape)
+        ref = O.backward(np.asfortranarray(data), hps)
+        own = bwd_need
+    with_copy = _raw(ps, fwd, data, g.work, need, cuda_device)
+    direct = _raw(ps, fwd, data, None, 0, cuda_device)
+    assert rel_l2(with_copy, ref) < 1e-5 and rel_l2(direct, ref) < 1e-5
+    assert rel_l2(with_copy, direct) < 1e-6
+    if own:
+        small = _raw(ps, fwd, data, g.work, own - 16, cuda_device)
+        assert (small == direct).all()
 
 
 def test_orbit_scratch_per_stream(cuda_device):
@@ -140,7 +174,7 @@ def test_orbit_scratch_per_stream(cuda_device):
 
     import gratopy_gb300 as gg
 
-    ps = device_settings(CFGS["bench_like"], cuda_device)
+    ps = device_settings(COPY_CFGS["copy_even"], cuda_device)
     sino = torch.rand(ps.sinogram_shape, device=cuda_device).T.contiguous().T
     a = gg.backprojection(sino, ps)
     side = torch.cuda.Stream(cuda_device)
@@ -161,7 +195,7 @@ def test_quarter_backprojection_is_deterministic(cuda_device):
     assert (a == b).all()
 
 
-@pytest.mark.parametrize("name", ["plain", "shifted_detector", "bench_like"])
+@pytest.mark.parametrize("name", ["plain", "shifted_detector", "bench_like", "copy_even"])
 def test_quarter_projections_in_solver_steps(cuda_device, name):
     """Landweber and TV agree with the per-angle kernels to float32 rounding;
     CG amplifies rounding, so it is held to the float32 solver bound of the
@@ -172,8 +206,9 @@ def test_quarter_projections_in_solver_steps(cuda_device, name):
     import gratopy_gb300 as gg
     from gratopy_gb300.phantom import random_ellipse_image
 
-    ps = device_settings(CFGS[name], cuda_device)
-    hps = host_settings(CFGS[name])
+    cfg = {**CFGS, **COPY_CFGS}[name]
+    ps = device_settings(cfg, cuda_device)
+    hps = host_settings(cfg)
     # a phantom's projection with 1% noise (a well-posed problem, as in the
     # solver parity tests)
     img = np.asfortranarray(random_ellipse_image(2, hps.img_shape[::-1]).T.astype(np.float64))
