@@ -618,7 +618,9 @@ def main():
                      "algorithmic_bytes": compulsory, "peak_source": hbm_kind,
                      "gather_bytes_per_s": 8 * pixel_angles() / t_dom / 1e9,
                      "issue_active_pct_ncu": issue,
-                     "note": "issue-bound gather: compulsory HBM bytes are 2.15 MB per launch"},
+                     "note": "issue- and L1-bound gather: compulsory HBM bytes are 2.15 MB per "
+                             "projection; the timed projection includes its orbit-copy "
+                             "pre-pass (one small kernel)"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"]},
         "gpu_launches": launches_per_step(ps) * steps,
