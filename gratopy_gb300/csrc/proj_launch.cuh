@@ -141,12 +141,23 @@ inline int bwd_split(const gr_geometry* g, int Nz) {
   return clamp_split(g, 8);
 }
 
-// float32 fan-beam single slices with a quarter-turn symmetric angle set:
-// one block row per base angle, four angles per lane group.  The kernel
-// keeps pixel offsets in 32 bits, so the slice must hold fewer than 2^31
-// pixels.
+inline int64_t pixel_angles(const gr_geometry* g) {
+  return (int64_t)g->Nx * g->Ny * g->Na;
+}
+
+// Stacks take the orbit kernels (one slice per block) from this many
+// pixel-angles per slice; smaller slices keep the 4-slice per-angle kernels,
+// which share each pixel-angle's geometry over 4 slices instead (measured,
+// Gpixel-angle/s forward / back: 512^2 x 360 orbit 922 / 1824, per-angle
+// 1033 / 1807; 1024^2 x 720 orbit 1318 / 2087, per-angle 1031 / 1868).
+constexpr int64_t kQuarterStackMin = 256ll << 20;
+
+// float32 fan beam with a quarter-turn symmetric angle set: one block row per
+// base angle, four angles per lane group, one slice per block.  Offsets within
+// a slice are 32-bit, so a slice holds fewer than 2^31 pixels.
 inline bool use_quarter(const gr_geometry* g, int Nz) {
-  return g->sym == 4 && g->dtype == GR_F32 && g->kind == GR_FANBEAM && Nz == 1 &&
+  return g->sym == 4 && g->dtype == GR_F32 && g->kind == GR_FANBEAM && Nz >= 1 &&
+         Nz <= 65535 && (Nz == 1 || pixel_angles(g) >= kQuarterStackMin) &&
          g->Na % 4 == 0 && g->Nx == g->Ny && (int64_t)g->Nx * g->Ny <= INT32_MAX;
 }
 
@@ -187,11 +198,11 @@ inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
 // 256^2 x 360).
 constexpr int64_t kQuarterFwdCopyMin = 48ll << 20;
 constexpr int64_t kQuarterBwdCopyMin = 12ll << 20;
+// slices copied per launch pair at most (a stack runs in chunks of as many
+// slices as the scratch holds)
+constexpr int kQuarterCopySlices = 8;
 
-inline int64_t pixel_angles(const gr_geometry* g) {
-  return (int64_t)g->Nx * g->Ny * g->Na;
-}
-
+// Bytes of one slice's copy (0: no copy for this geometry).
 inline size_t quarter_fwd_bytes(const gr_geometry* g, int Nz) {
   if (!use_quarter(g, Nz) || pixel_angles(g) < kQuarterFwdCopyMin) return 0;
   return (size_t)g->Nx * (size_t)g->Ny * sizeof(float4);
@@ -204,21 +215,27 @@ inline size_t quarter_bwd_bytes(const gr_geometry* g, int Nz) {
 
 inline size_t orbit_work_bytes(const gr_geometry* g, int Nz) {
   const size_t f = quarter_fwd_bytes(g, Nz), b = quarter_bwd_bytes(g, Nz);
-  return f > b ? f : b;
+  const int slices = Nz < kQuarterCopySlices ? Nz : kQuarterCopySlices;
+  return (f > b ? f : b) * (size_t)(slices > 0 ? slices : 0);
 }
 
-// The caller's scratch holds `need` bytes on a 16-byte boundary.
-inline bool work_fits(const gr_geometry* g, size_t need) {
-  return need > 0 && g->work != nullptr && g->work_bytes >= need &&
-         (reinterpret_cast<uintptr_t>(g->work) & 15u) == 0;
+// Slices per launch pair that the caller's scratch holds (16-byte aligned)
+// for copies of `per_slice` bytes; 0: no copy.
+inline int work_slices(const gr_geometry* g, size_t per_slice, int Nz) {
+  if (per_slice == 0 || g->work == nullptr || (reinterpret_cast<uintptr_t>(g->work) & 15u) != 0)
+    return 0;
+  const size_t n = g->work_bytes / per_slice;
+  return n >= (size_t)Nz ? Nz : (int)n;
 }
+
 
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   const int ZB = zblock(Nz);
   const int group = g->dtype == GR_F32 ? fast::kRayGroup : 1;  // bins per lane group
   const int per_block = (32 / split) * (kFwdBlock / 32) * group;
-  const int angles = use_quarter(g, Nz) ? g->Na / 4 : g->Na;
-  return dim3((g->Ns + per_block - 1) / per_block, angles, (Nz + ZB - 1) / ZB);
+  if (use_quarter(g, Nz))  // one slice per block
+    return dim3((g->Ns + per_block - 1) / per_block, g->Na / 4, Nz);
+  return dim3((g->Ns + per_block - 1) / per_block, g->Na, (Nz + ZB - 1) / ZB);
 }
 
 inline fast::QuarterMaps quarter_maps(const gr_geometry* g) {
@@ -237,7 +254,7 @@ inline fast::QuarterMaps quarter_maps(const gr_geometry* g) {
 inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
   if (use_quarter_bwd(g, Nz)) {  // 32 x (8 / split) tiles of the quadrant x, y < N/2
     const int half = g->Nx / 2, rows = kBwdTileSlow / split;
-    return dim3((half + kBwdTileFast - 1) / kBwdTileFast, (half + rows - 1) / rows, 1);
+    return dim3((half + kBwdTileFast - 1) / kBwdTileFast, (half + rows - 1) / rows, Nz);
   }
   const int ZB = zblock(Nz);
   const int fast = io == ORDER_F ? g->Nx : g->Ny;
@@ -256,19 +273,28 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
     if (g->kind == GR_RADON) {
       fast::radon_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
           img, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi, partials, skip);
-    } else if (ZB == 1 && use_quarter(g, Nz)) {
+    } else if (use_quarter(g, Nz)) {
       const float* ofs = static_cast<const float*>(g->ofs);
       const float* sdpd = static_cast<const float*>(g->sdpd);
       const fast::QuarterMaps qm = quarter_maps(g);
-      if (work_fits(g, quarter_fwd_bytes(g, Nz))) {
+      const int chunk = work_slices(g, quarter_fwd_bytes(g, Nz), Nz);
+      if (chunk > 0) {
+        // slices in chunks: orbit-pixel copies, then the forward on them;
+        // each chunk's block partials follow the previous chunk's
         float4* img4 = static_cast<float4*>(g->work);
-        const dim3 pgrid((g->Nx + 255) / 256, g->Ny);
-        fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, skip);
-        fast::fan_fwd_quarter<SO, IO, SPLIT, true, Epi><<<grid, kFwdBlock, 0, st>>>(
-            img, img4, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi, partials, skip);
+        const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
+        for (int z0 = 0; z0 < Nz; z0 += chunk) {
+          const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;
+          const dim3 pgrid((g->Nx + 255) / 256, g->Ny, zc);
+          fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, z0, skip);
+          fast::fan_fwd_quarter<SO, IO, SPLIT, true, Epi>
+              <<<dim3(grid.x, grid.y, zc), kFwdBlock, 0, st>>>(
+                  img, img4, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi,
+                  partials ? partials + z0 * per_slice_blocks : nullptr, skip, z0);
+        }
       } else {
         fast::fan_fwd_quarter<SO, IO, SPLIT, false, Epi><<<grid, kFwdBlock, 0, st>>>(
-            img, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi, partials, skip);
+            img, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi, partials, skip, 0);
       }
     } else {
       fast::fan_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
@@ -329,20 +355,28 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
     // blocks (a 512^2 image then fits in one wave of resident blocks)
     constexpr int PY = (SPLIT == 1 && ZB == 1) ? 2 : 1;
     const dim3 fblock(kBwdTileFast, kBwdTileSlow / PY);
-    if (ZB == 1 && use_quarter_bwd(g, Nz)) {
+    if (use_quarter_bwd(g, Nz)) {
       const float* ofs = static_cast<const float*>(g->ofs);
       const float* sdpd = static_cast<const float*>(g->sdpd);
-      if (work_fits(g, quarter_bwd_bytes(g, Nz))) {
+      const int chunk = work_slices(g, quarter_bwd_bytes(g, Nz), Nz);
+      if (chunk > 0) {
+        // slices in chunks: interleaved row copies, then the backprojection
+        // on them; each chunk's block partials follow the previous chunk's
         float4* rows4 = static_cast<float4*>(g->work);
-        const dim3 rgrid((g->Ns + 255) / 256, g->Na / 4);
-        fast::orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, sdpd, d, rows4, skip);
-        fast::fan_bwd_orbit<IO, SO, SPLIT, true, Epi><<<grid, block, 0, st>>>(
-            sino, rows4, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials,
-            skip);
+        const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
+        for (int z0 = 0; z0 < Nz; z0 += chunk) {
+          const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;
+          const dim3 rgrid((g->Ns + 255) / 256, g->Na / 4, zc);
+          fast::orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, sdpd, d, rows4, z0, skip);
+          fast::fan_bwd_orbit<IO, SO, SPLIT, true, Epi>
+              <<<dim3(grid.x, grid.y, zc), block, 0, st>>>(
+                  sino, rows4, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi,
+                  partials ? partials + z0 * per_slice_blocks : nullptr, skip, z0);
+        }
       } else {
         fast::fan_bwd_orbit<IO, SO, SPLIT, false, Epi><<<grid, block, 0, st>>>(
             sino, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials,
-            skip);
+            skip, 0);
       }
     } else if (g->kind == GR_RADON) {
       fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, fblock, 0, st>>>(

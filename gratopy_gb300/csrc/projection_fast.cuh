@@ -16,6 +16,8 @@
 // float64 keeps the reference-order kernels of projection.cuh.
 #pragma once
 
+#include <type_traits>
+
 #include "projection.cuh"
 
 namespace gr {
@@ -781,14 +783,17 @@ struct QuarterMaps {
   int axx[3], axy[3], ayx[3], ayy[3], cx[3], cy[3];
 };
 
+// img (and img4) point at slice z; offsets within a slice are 32-bit except
+// for C-ordered images, whose slices interleave.
 template <int SO, int IO, int SPLIT, bool PIX4, class Epi>
 __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__ img,
                                                        const float4* __restrict__ img4,
                                                        const float* __restrict__ ofs,
                                                        const float* __restrict__ sdpd,
                                                        FanGeo<float> g, Dims d, QuarterMaps qm,
-                                                       Epi epi, uint3 bid) {
+                                                       Epi epi, uint3 bid, int64_t z) {
   constexpr int kOrbit = 4;
+  using Off = typename std::conditional<IO == ORDER_C && !PIX4, int64_t, int>::type;
   const GroupLayout<SPLIT> L(bid);
   const int64_t s0 = L.s0;
   const int64_t a = bid.y;              // base angle in [0, Na/4)
@@ -823,13 +828,12 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
       sy = d.Nx;
     }
     // element steps of the turned pixels along the array's x and y axes
-    // (32-bit: a single slice of at most 2^31 pixels)
-    int mstep_x[kOrbit - 1], mstep_y[kOrbit - 1], mbase[kOrbit - 1];
+    Off mstep_x[kOrbit - 1], mstep_y[kOrbit - 1], mbase[kOrbit - 1];
 #pragma unroll
     for (int m = 0; m < kOrbit - 1; ++m) {
-      mstep_x[m] = (int)(qm.axx[m] * sx + qm.ayx[m] * sy);
-      mstep_y[m] = (int)(qm.axy[m] * sx + qm.ayy[m] * sy);
-      mbase[m] = (int)(qm.cx[m] * sx + qm.cy[m] * sy);
+      mstep_x[m] = (Off)(qm.axx[m] * sx + qm.ayx[m] * sy);
+      mstep_y[m] = (Off)(qm.axy[m] * sx + qm.ayy[m] * sy);
+      mbase[m] = (Off)(qm.cx[m] * sx + qm.cy[m] * sy);
     }
     int64_t step_x = sx, step_y = sy;
     const bool steep = fabsf(dpx) < fabsf(dpy) && fabsf(dmx) < fabsf(dmy);
@@ -848,7 +852,7 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
       step_y = sx;
 #pragma unroll
       for (int m = 0; m < kOrbit - 1; ++m) {
-        const int t2 = mstep_x[m];
+        const Off t2 = mstep_x[m];
         mstep_x[m] = mstep_y[m];
         mstep_y[m] = t2;
       }
@@ -874,9 +878,9 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
       const float xlf = (float)xlo;
       float t = fmaf(ddx, xlf, fmaf(ddy, yf, t_c));
       float ss = fmaf(dx, xlf, fmaf(dy, yf, s_c));
-      const int stp = (int)step_x;
-      int o0 = (int)(y * step_y + xlo * step_x);
-      int om[kOrbit - 1];
+      const Off stp = (Off)step_x;
+      Off o0 = (Off)(y * step_y + xlo * step_x);
+      Off om[kOrbit - 1];
       if constexpr (!PIX4) {
 #pragma unroll
         for (int m = 0; m < kOrbit - 1; ++m) om[m] = mbase[m] + y * mstep_y[m] + xlo * mstep_x[m];
@@ -928,7 +932,7 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
 #pragma unroll
         for (int m = 0; m < kOrbit; ++m) {
           const int64_t am = a + m * quarter;
-          part += epi(s, am, 0, sino_index<SO>(s, am, 0, d), acc[m][q] * sc);
+          part += epi(s, am, z, sino_index<SO>(s, am, z, d), acc[m][q] * sc);
         }
       }
     }
@@ -938,34 +942,37 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
 
 // The four pixels a candidate of the orbit-sharing forward projection loads,
 // as one float4 per pixel: img4[x + Nx y] = (img(P), img(M_1 P), img(M_2 P),
-// img(M_3 P)) for P = (x, y) and the quarter-turn index maps M_m.
+// img(M_3 P)) for P = (x, y) and the quarter-turn index maps M_m; slice
+// z0 + blockIdx.z goes to copy blockIdx.z.
 template <int IO>
 __global__ void __launch_bounds__(256)
 orbit_pixels(const float* __restrict__ img, Dims d, QuarterMaps qm, float4* __restrict__ img4,
-             const int* __restrict__ skip) {
+             int64_t z0, const int* __restrict__ skip) {
   if (skip != nullptr && *skip) return;
   const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t y = blockIdx.y;
+  const int64_t z = z0 + blockIdx.z;
   if (x >= d.Nx) return;
   float v[4];
-  v[0] = ldg(img + img_index<IO>(x, y, 0, d));
+  v[0] = ldg(img + img_index<IO>(x, y, z, d));
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
     const int64_t mx = qm.cx[m] + qm.axx[m] * x + qm.axy[m] * y;
     const int64_t my = qm.cy[m] + qm.ayx[m] * x + qm.ayy[m] * y;
-    v[m + 1] = ldg(img + img_index<IO>(mx, my, 0, d));
+    v[m + 1] = ldg(img + img_index<IO>(mx, my, z, d));
   }
-  img4[x + d.Nx * y] = make_float4(v[0], v[1], v[2], v[3]);
+  img4[((int64_t)blockIdx.z * d.Ny + y) * d.Nx + x] = make_float4(v[0], v[1], v[2], v[3]);
 }
 
 // The four sinogram rows of every quarter-turn orbit of angles, premultiplied
 // by sdpd, as one float4 per (base angle, bin): rows4[a Ns + s] =
 // sdpd[s] (sino[s, a], sino[s, a + Q], sino[s, a + 2Q], sino[s, a + 3Q]),
-// Q = Na / 4.  Lanes run along the bins (coalesced for F-ordered sinograms).
+// Q = Na / 4.  Lanes run along the bins (coalesced for F-ordered sinograms);
+// slice z0 + blockIdx.z goes to copy blockIdx.z.
 template <int SO>
 __global__ void __launch_bounds__(256)
 orbit_rows(const float* __restrict__ sino, const float* __restrict__ sdpd, Dims d,
-           float4* __restrict__ rows4, const int* __restrict__ skip) {
+           float4* __restrict__ rows4, int64_t z0, const int* __restrict__ skip) {
   if (skip != nullptr && *skip) return;
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t a = blockIdx.y;
@@ -973,10 +980,11 @@ orbit_rows(const float* __restrict__ sino, const float* __restrict__ sdpd, Dims 
   int64_t ss_, sa_, sz_;
   sino_strides<SO>(d, ss_, sa_, sz_);
   const int64_t Q = d.Na / 4;
-  const float* p = sino + s * ss_ + a * sa_;
+  const float* p = sino + s * ss_ + a * sa_ + (z0 + blockIdx.z) * sz_;
   const float w = ldg(sdpd + s);
-  rows4[a * d.Ns + s] = make_float4(w * ldg(p), w * ldg(p + Q * sa_), w * ldg(p + 2 * Q * sa_),
-                                    w * ldg(p + 3 * Q * sa_));
+  rows4[((int64_t)blockIdx.z * Q + a) * d.Ns + s] =
+      make_float4(w * ldg(p), w * ldg(p + Q * sa_), w * ldg(p + 2 * Q * sa_),
+                  w * ldg(p + 3 * Q * sa_));
 }
 
 // Backprojection over quarter-turn pixel orbits.  With the maps powers of
@@ -997,7 +1005,7 @@ __global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
 fan_bwd_orbit(const float* __restrict__ sino, const float4* __restrict__ rows4,
               const float* __restrict__ ofs, const float* __restrict__ sdpd, FanGeo<float> gg,
               Dims d, QuarterMaps qm, Epi epi, double* __restrict__ partials,
-              const int* __restrict__ skip) {
+              const int* __restrict__ skip, int64_t z0) {
   constexpr int kOrbit = 4;
   constexpr int kRowsT = kBwdTileSlow / G;  // quadrant rows of the block tile
   __shared__ double red[32];
@@ -1029,7 +1037,13 @@ fan_bwd_orbit(const float* __restrict__ sino, const float4* __restrict__ rows4,
   const float mid_det = gg.mid_det;
   int64_t ss_, sa_, sz_;
   sino_strides<SO>(d, ss_, sa_, sz_);
-  const int ss = (int)ss_, sa = (int)sa_;  // a slice of fewer than 2^31 values
+  // slice z of the sinogram (and its row copy); offsets within an F-ordered
+  // slice are 32-bit, C-ordered slices interleave
+  using Off = typename std::conditional<SO == ORDER_C, int64_t, int>::type;
+  const Off ss = (Off)ss_, sa = (Off)sa_;
+  const int64_t z = z0 + blockIdx.z;
+  sino += z * sz_;
+  if constexpr (ROWS4) rows4 += (int64_t)blockIdx.z * (d.Na / kOrbit) * d.Ns;
   const int Ns = (int)d.Ns;
   float acc[kOrbit];
 #pragma unroll
@@ -1115,7 +1129,7 @@ fan_bwd_orbit(const float* __restrict__ sino, const float4* __restrict__ rows4,
   if (own && grp == 0) {
 #pragma unroll
     for (int k = 0; k < kOrbit; ++k)
-      part += epi(ox[k], oy[k], 0, img_index<IO>(ox[k], oy[k], 0, d), acc[k]);
+      part += epi(ox[k], oy[k], z, img_index<IO>(ox[k], oy[k], z, d), acc[k]);
   }
   if (Epi::kReduce) {
     const double t = block_sum(part, red);
@@ -1128,12 +1142,16 @@ __global__ void __launch_bounds__(kFwdBlock)
 fan_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4,
                 const float* __restrict__ ofs,
                 const float* __restrict__ sdpd, FanGeo<float> g, Dims d, QuarterMaps qm, Epi epi,
-                double* __restrict__ partials, const int* __restrict__ skip) {
+                double* __restrict__ partials, const int* __restrict__ skip, int64_t z0) {
   __shared__ double red[32];
   if (skip != nullptr && *skip) return;
-  const double part =
-      fan_fwd_quarter_tile<SO, IO, SPLIT, PIX4, Epi>(img, img4, ofs, sdpd, g, d, qm, epi,
-                                                     blockIdx);
+  // slice z of the image, copy blockIdx.z of the orbit pixels
+  const int64_t z = z0 + blockIdx.z;
+  int64_t sx, sy, sz;
+  img_strides<IO>(d, sx, sy, sz);
+  const float4* img4z = PIX4 ? img4 + (int64_t)blockIdx.z * d.Nx * d.Ny : nullptr;
+  const double part = fan_fwd_quarter_tile<SO, IO, SPLIT, PIX4, Epi>(
+      img + z * sz, img4z, ofs, sdpd, g, d, qm, epi, blockIdx, z);
   if (Epi::kReduce) {
     double t = block_sum(part, red);
     if (threadIdx.x + blockDim.x * threadIdx.y == 0)

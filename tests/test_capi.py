@@ -105,6 +105,12 @@ def test_host_only_entry_points(library):
     assert sized(512, 4000, 400) == 100 * 4000 * 16
     assert sized(256, 384, 360) == 90 * 384 * 16  # the backprojection's only
     assert sized(128, 192, 360) == 0
+    # stacks (from 256 * 2^20 pixel-angles per slice): one slice's copy per
+    # slice, up to 8 slices per launch pair; smaller slices keep the
+    # per-angle kernels
+    sized(1024, 1536, 720)
+    assert work(ctypes.byref(q), 3) == 3 * 1024 * 1024 * 16
+    assert work(ctypes.byref(q), 20) == 8 * 1024 * 1024 * 16
     sized(512, 768, 360)
     assert work(ctypes.byref(q), 3) == 0
     q.dtype = 1

@@ -169,6 +169,91 @@ def test_orbit_scratch_and_direct_gather_agree(cuda_device, name, fwd):
         assert (small == direct).all()
 
 
+# a stack whose slices take the orbit kernels (from 256 * 2^20 pixel-angles
+# per slice); one slice of copy per launch pair unless the scratch holds more
+STACK_CFG = dict(geometry="fanbeam", img_shape=(768, 768), angles=480, n_detectors=1100,
+                 detector_width=400.0, R=400.0, RE=200.0)
+
+
+def _stack_call(ps, fwd, x, nz, order, work, work_bytes, cuda_device, sym=4):
+    import ctypes
+
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import _lib, core
+
+    g = _lib.GrGeometry.from_buffer_copy(ps.gr_geometry(np.float32))
+    g.sym, g.work, g.work_bytes = sym, work, work_bytes
+    shape = (ps.sinogram_shape if fwd else ps.img_shape) + (nz,)
+    out = gg.core.empty(shape, torch.float32, order, cuda_device)
+    of = core._oflag(order)
+    _lib.call("gr_forward" if fwd else "gr_backward", ctypes.byref(g), core._ptr(out),
+              core._ptr(x), nz, of, of, core._stream_ptr(cuda_device))
+    return out
+
+
+@pytest.mark.parametrize("order", ["F", "C"])
+@pytest.mark.parametrize("fwd", [True, False])
+def test_orbit_kernels_on_stacks(cuda_device, order, fwd):
+    """Slices of a stack in chunks of 1, 2 and 3 slices of scratch and without
+    scratch agree with each other, with the per-angle 4-slice kernels, and
+    (first and last slice) with the oracle."""
+    import ctypes
+
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import _lib
+
+    nz = 3
+    ps = device_settings(STACK_CFG, cuda_device)
+    hps = host_settings(STACK_CFG)
+    g = ps.gr_geometry(np.float32)
+    per_slice = int(_lib.raw("gr_work_bytes")(ctypes.byref(g), 1))
+    assert per_slice > 0 and int(_lib.raw("gr_work_bytes")(ctypes.byref(g), nz)) == nz * per_slice
+    buf = torch.empty(nz * per_slice, dtype=torch.uint8, device=cuda_device)
+    in_shape = (ps.img_shape if fwd else ps.sinogram_shape) + (nz,)
+    data = np.random.default_rng(8).random(in_shape)
+    x = gg.core.empty(in_shape, torch.float32, order, cuda_device)
+    x.copy_(torch.from_numpy(data.astype(np.float32)))
+    runs = {k: _stack_call(ps, fwd, x, nz, order, buf.data_ptr(), k * per_slice, cuda_device)
+            for k in (1, 2, 3)}
+    direct = _stack_call(ps, fwd, x, nz, order, None, 0, cuda_device)
+    per_angle = _stack_call(ps, fwd, x, nz, order, None, 0, cuda_device, sym=0)
+    assert torch.equal(runs[1], runs[2]) and torch.equal(runs[1], runs[3])
+    d = direct.double().cpu().numpy()
+    r = runs[1].double().cpu().numpy()
+    assert rel_l2(r, d) < 1e-6
+    assert rel_l2(r, per_angle.double().cpu().numpy()) < 4e-6
+    for k in (0, nz - 1):
+        sl = np.asfortranarray(data[:, :, k])
+        ref = O.forward(sl, hps) if fwd else O.backward(sl, hps)
+        assert rel_l2(r[:, :, k], ref) < 1e-5
+
+
+def test_orbit_stack_solver_partials(cuda_device):
+    """CG's fused reductions on a stack run in per-slice chunks: the block
+    partials of every chunk land after the previous chunk's."""
+    import torch
+
+    import gratopy_gb300 as gg
+
+    nz = 2
+    ps = device_settings(STACK_CFG, cuda_device)
+    rng = np.random.default_rng(9)
+    img = gg.core.empty(ps.img_shape + (nz,), torch.float32, "F", cuda_device)
+    img.copy_(torch.from_numpy(rng.random(ps.img_shape + (nz,)).astype(np.float32)))
+    sino = gg.forwardprojection(img, ps)
+    g = ps.gr_geometry(np.float32)
+    res = {}
+    for sym in (4, 0):
+        g.sym = sym
+        res[sym] = gg.conjugate_gradients(sino, ps, 4).double().cpu().numpy()
+    g.sym = 4
+    assert rel_l2(res[4], res[0]) < 1e-5
+
+
 def test_orbit_scratch_per_stream(cuda_device):
     import torch
 
