@@ -274,27 +274,43 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
       fast::radon_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
           img, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi, partials, skip);
     } else if (use_quarter(g, Nz)) {
+      // one launch per slice on its base pointers (grid.z of fwd_grid counts
+      // the slices; each launch's block partials follow the previous slice's)
       const float* ofs = static_cast<const float*>(g->ofs);
       const float* sdpd = static_cast<const float*>(g->sdpd);
       const fast::QuarterMaps qm = quarter_maps(g);
+      const dim3 sgrid(grid.x, grid.y, 1);
+      const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
+      int64_t sx, sy, sz;
+      img_strides<IO>(d, sx, sy, sz);
       const int chunk = work_slices(g, quarter_fwd_bytes(g, Nz), Nz);
       if (chunk > 0) {
-        // slices in chunks: orbit-pixel copies, then the forward on them;
-        // each chunk's block partials follow the previous chunk's
+        // slices in chunks: orbit-pixel copies, then the forward on them
         float4* img4 = static_cast<float4*>(g->work);
-        const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
+        const int64_t slice4 = (int64_t)g->Nx * g->Ny;
         for (int z0 = 0; z0 < Nz; z0 += chunk) {
           const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;
-          const dim3 pgrid((g->Nx + 255) / 256, g->Ny, zc);
-          fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, z0, skip);
-          fast::fan_fwd_quarter<SO, IO, SPLIT, true, Epi>
-              <<<dim3(grid.x, grid.y, zc), kFwdBlock, 0, st>>>(
-                  img, img4, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi,
-                  partials ? partials + z0 * per_slice_blocks : nullptr, skip, z0);
+          if constexpr (IO == ORDER_F) {
+            constexpr int kTile = fast::kOrbitTile;
+            const dim3 tgrid((g->Nx + kTile - 1) / kTile, (g->Ny + kTile - 1) / kTile, zc);
+            fast::orbit_pixels_tiled<IO><<<tgrid, dim3(kTile, kTile), 0, st>>>(img, d, qm,
+                                                                               img4, z0, skip);
+          } else {
+            const dim3 pgrid((g->Nx + 255) / 256, g->Ny, zc);
+            fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, z0, skip);
+          }
+          for (int k = 0; k < zc; ++k) {
+            const int64_t z = z0 + k;
+            fast::fan_fwd_quarter<SO, IO, SPLIT, true, Epi><<<sgrid, kFwdBlock, 0, st>>>(
+                img + z * sz, img4 + k * slice4, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi,
+                partials ? partials + z * per_slice_blocks : nullptr, skip, z);
+          }
         }
       } else {
-        fast::fan_fwd_quarter<SO, IO, SPLIT, false, Epi><<<grid, kFwdBlock, 0, st>>>(
-            img, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi, partials, skip, 0);
+        for (int64_t z = 0; z < Nz; ++z)
+          fast::fan_fwd_quarter<SO, IO, SPLIT, false, Epi><<<sgrid, kFwdBlock, 0, st>>>(
+              img + z * sz, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi,
+              partials ? partials + z * per_slice_blocks : nullptr, skip, z);
       }
     } else {
       fast::fan_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
