@@ -59,7 +59,8 @@ typedef struct gr_geometry {
   double geo[11];
   /* Launch shape (0 = automatic): lanes per detector bin in the forward
    * projection and angle groups per pixel in the backprojection; each must
-   * be 1, 2, 4 or 8.  Chosen by the autotuner. */
+   * be 1, 2, 4 or 8.  Chosen by the autotuner.  The quarter-turn forward
+   * (sym = 4) runs twice fwd_split lanes per group of bins. */
   int fwd_split, bwd_split;
   /* Quarter-turn symmetry (no counterpart in the reference): 4 when the
    * angles a + m*Na/4 see the (square, centred) pixel grid as angle a sees it
