@@ -68,7 +68,13 @@ def order_of(t: torch.Tensor) -> str:
     """'C' if C-contiguous (checked first, as gratopy does), 'F' if Fortran-contiguous."""
     if t.is_contiguous():
         return "C"
-    if t.permute(*reversed(range(t.dim()))).is_contiguous():
+    # Fortran order: first index fastest (strides of size-1 dims do not matter)
+    expected = 1
+    for n, st in zip(t.shape, t.stride()):
+        if n != 1 and st != expected:
+            break
+        expected *= n
+    else:
         return "F"
     raise ValueError(
         f"tensor of shape {tuple(t.shape)} with strides {t.stride()} is neither C- nor "
@@ -365,16 +371,16 @@ class ProjectionSettings:
         self.ensure_dtype(dtype)
         return self._dev[_np_dtype(dtype)]
 
-    def gr_geometry(self, dtype) -> _lib.GrGeometry:
+    def gr_geometry(self, dtype, stream=None) -> _lib.GrGeometry:
         """C-ABI geometry descriptor for precision ``dtype`` (tables uploaded).
 
-        The descriptor carries the scratch of the current stream (see
-        :meth:`_bind_work`); a descriptor kept across calls on several
-        streams at once must be fetched again on each stream.
+        The descriptor carries the scratch of ``stream`` (default: the current
+        stream; see :meth:`_bind_work`); a descriptor kept across calls on
+        several streams at once must be fetched again on each stream.
         """
         self.ensure_dtype(dtype)
         dt = _np_dtype(dtype)
-        return self._bind_work(self._geom[dt], dt)
+        return self._bind_work(self._geom[dt], dt, stream)
 
     def gr_geometry_adjoint(self, dtype) -> _lib.GrGeometry:
         """Descriptor whose backprojection is the plain transpose of the forward projection."""
@@ -382,15 +388,17 @@ class ProjectionSettings:
         dt = _np_dtype(dtype)
         return self._bind_work(self._geom_adj[dt], dt)
 
-    def _bind_work(self, g, dt):
-        """Point ``g.work`` at this settings object's scratch for the current
-        stream (allocated on first use; the library uses it stream-ordered).
-        During a stream capture the descriptor keeps the scratch bound before
-        the capture, the one of the stream that replays the graph."""
+    def _bind_work(self, g, dt, stream=None):
+        """Point ``g.work`` at this settings object's scratch for ``stream``
+        (default: the current one; allocated on first use, used by the library
+        stream-ordered).  During a stream capture the descriptor keeps the
+        scratch bound before the capture, the one of the stream that replays
+        the graph."""
         nbytes = self._work_bytes.get(dt, 0)
         if not nbytes or torch.cuda.is_current_stream_capturing():
             return g
-        stream = torch.cuda.current_stream(self.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device)
         key = (dt, stream.cuda_stream)
         buf = self._work.get(key)
         if buf is None:
@@ -518,15 +526,25 @@ def _event(device):
     return ev
 
 
-def _project(entry, out, inp, out_order, in_order, ps):
+def _project(entry, out, inp, out_order, in_order, ps, event=True):
     """One projection through the settings' geometry descriptor: the tuned
-    launch shape and, for quarter-turn symmetric fan-beam angle sets, the
-    orbit-sharing forward kernel apply."""
-    g = ps.gr_geometry(_np_dtype(out.dtype))
-    with torch.cuda.device(out.device):
-        _lib.call(entry, ctypes.byref(g), _ptr(out), _ptr(inp), _nz(out), _oflag(out_order),
-                  _oflag(in_order), _stream_ptr(out.device))
-        return _event(out.device)
+    launch shape, the quarter-turn orbit kernels and the current stream's
+    scratch apply.  Returns a CUDA event recorded after it, or None."""
+    dev = out.device
+    stream = torch.cuda.current_stream(dev)
+    g = ps.gr_geometry(_np_dtype(out.dtype), stream)
+    args = (entry, ctypes.byref(g), _ptr(out), _ptr(inp), _nz(out), _oflag(out_order),
+            _oflag(in_order), ctypes.c_void_p(stream.cuda_stream))
+    if dev.index == torch.cuda.current_device():
+        _lib.call(*args)
+    else:
+        with torch.cuda.device(dev):
+            _lib.call(*args)
+    if not event:
+        return None
+    ev = torch.cuda.Event()
+    ev.record(stream)
+    return ev
 
 
 def radon(sino, img, projectionsetting, wait_for=[]):
@@ -569,7 +587,12 @@ def forwardprojection(img, projectionsetting, sino=None, wait_for=[]):
         z = (img.shape[2],) if img.dim() > 2 else ()
         sino = empty(tuple(projectionsetting.sinogram_shape) + z, img.dtype,
                      "C" if img.is_contiguous() else "F", img.device)
-    projectionsetting.forwardprojection(sino, img, projectionsetting, wait_for=wait_for)
+    if type(projectionsetting).forwardprojection is ProjectionSettings.forwardprojection:
+        # the settings' own method without its (discarded) event
+        io, so = _prepare(img, sino, projectionsetting)
+        _project("gr_forward", sino, img, so, io, projectionsetting, event=False)
+    else:
+        projectionsetting.forwardprojection(sino, img, projectionsetting, wait_for=wait_for)
     return sino
 
 
@@ -580,7 +603,12 @@ def backprojection(sino, projectionsetting, img=None, wait_for=[]):
         z = (sino.shape[2],) if sino.dim() > 2 else ()
         img = empty(tuple(projectionsetting.img_shape) + z, sino.dtype,
                     "C" if sino.is_contiguous() else "F", sino.device)
-    projectionsetting.backprojection(img, sino, projectionsetting, wait_for=wait_for)
+    if type(projectionsetting).backprojection is ProjectionSettings.backprojection:
+        # the settings' own method without its (discarded) event
+        io, so = _prepare(img, sino, projectionsetting)
+        _project("gr_backward", img, sino, io, so, projectionsetting, event=False)
+    else:
+        projectionsetting.backprojection(img, sino, projectionsetting, wait_for=wait_for)
     return img
 
 
