@@ -272,6 +272,26 @@ def test_orbit_scratch_per_stream(cuda_device):
     assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("size", ["small", "copy"])
+def test_orbit_kernels_apply_each_angles_own_weight(cuda_device, size):
+    """Random angle weights (equispaced angles otherwise weigh alike): every
+    row a + j Na/4 of the orbit backprojection carries its own angle's
+    weight, with and without the row copy, in the solver epilogues too."""
+    base = CFGS["shifted_detector"] if size == "small" else COPY_CFGS["copy_even"]
+    na = base["angles"]
+    cfg = dict(base, angle_weights=np.random.default_rng(12).uniform(0.5, 1.5, na))
+    ps = device_settings(cfg, cuda_device)
+    hps = host_settings(cfg)
+    g = ps.gr_geometry(np.float32)
+    assert g.sym == 4 and (bool(g.work) == (size == "copy"))
+    sino = np.random.default_rng(13).random(ps.sinogram_shape)
+    ref = O.backward(np.asfortranarray(sino), hps)
+    shared = _backward(ps, sino, "F", 4, 0, cuda_device)
+    direct = _backward(ps, sino, "F", 0, 0, cuda_device)
+    assert rel_l2(shared, ref) < 1e-5
+    assert rel_l2(shared, direct) < 4e-6
+
+
 def test_quarter_backprojection_is_deterministic(cuda_device):
     ps = device_settings(CFGS["bench_like"], cuda_device)
     sino = np.random.default_rng(4).random(ps.sinogram_shape)
