@@ -121,6 +121,22 @@ def test_host_only_entry_points(library):
                                  (0, 1, -1, 0, 0, c)]) == 512 * 512 * 16
     set_maps(0, [(0,) * 6] * 3)
     assert work(ctypes.byref(q), 1) == 0
+    # block-partial counts of the fused reductions follow the orbit grids:
+    # the forward runs 2 * fwd_split lanes per group of 4 bins in 128-thread
+    # blocks over Na/4 base angles, one slice per launch; the backprojection
+    # 32 x (8 / bwd_split) tiles of the quadrant, one slice per block
+    fwd_parts, bwd_parts = lib.gr_forward_partials, lib.gr_backward_partials
+    sized(512, 768, 360)
+    cases = {(8, 8): (24 * 90, 8 * 256), (4, 2): (12 * 90, 8 * 64), (1, 1): (3 * 90, 8 * 32)}
+    for (fs, bs), (want_f, want_b) in cases.items():
+        q.fwd_split, q.bwd_split = fs, bs
+        assert fwd_parts(ctypes.byref(q), 1) == want_f
+        assert bwd_parts(ctypes.byref(q), 1, 0) == want_b
+    sized(1024, 1536, 720)  # a stack whose slices take the orbit kernels
+    q.fwd_split, q.bwd_split = 8, 8
+    assert fwd_parts(ctypes.byref(q), 3) == 48 * 180 * 3
+    assert bwd_parts(ctypes.byref(q), 3, 0) == 16 * 512 * 3
+    q.fwd_split = q.bwd_split = 0
     assert lib.gr_forward_partials(None, 1) == 0
     # descriptors: binding layouts equal the library's
     assert lib.gr_geometry_size() == ctypes.sizeof(_lib.GrGeometry)
