@@ -72,18 +72,21 @@ typedef struct gr_geometry {
   int sym;
   int sym_map[3][6];
   /* Device scratch (no counterpart in the reference) that a call may use
-   * while it runs, stream-ordered: the fan-beam backprojection over
-   * quarter-turn orbits keeps an interleaved copy of the four sinogram rows
-   * of every angle orbit there (gr_work_bytes gives the size).  NULL or
-   * smaller than that: the kernels read the sinogram directly.  Calls that
-   * may run at the same time must not share it. */
+   * while it runs, stream-ordered, 16-byte aligned: the quarter-turn orbit
+   * kernels keep interleaved copies of their input there (the forward: the
+   * four orbit pixels of every pixel; the backprojection: the four sinogram
+   * rows of every angle orbit).  gr_work_bytes gives the size for a number
+   * of slices; a stack is copied in chunks of as many slices as the scratch
+   * holds.  NULL or smaller than one slice's copy: the kernels read their
+   * input directly.  Calls that may run at the same time must not share
+   * it. */
   void* work;
   size_t work_bytes;
 } gr_geometry;
 
 GR_API const char* gr_error_string(int code);
-/* Scratch bytes the projections of g on Nz slices can use (gr_geometry.work);
- * 0 when they use none. */
+/* Scratch bytes the projections of g on Nz slices can use (gr_geometry.work;
+ * at most 8 slices' copies); 0 when they use none. */
 GR_API size_t gr_work_bytes(const gr_geometry* g, int Nz);
 /* sizeof(gr_geometry), for bindings that mirror the struct. */
 GR_API size_t gr_geometry_size(void);
