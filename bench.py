@@ -50,6 +50,10 @@ UNIT = "Gpixel-angle/s"
 WORKLOAD = dict(geometry="fanbeam", img_shape=(512, 512), angles=360, n_detectors=768,
                 detector_width=400.0, RE=200.0, R=400.0,
                 image_width=0.9 * (2 * 0.5 * 200.0 / np.sqrt(1 + 0.25)))
+# Radon 256 x 256, 180 angles over [0, pi), 363 detectors of width
+# 2 sqrt(2) / 363 (the detector spans the image diagonal), image width 2
+RADON_WORKLOAD = dict(geometry="radon", img_shape=(256, 256), angles=180, n_detectors=363,
+                      detector_width=2.0 * np.sqrt(2.0), image_width=2.0)
 SEED = 1234
 
 
@@ -290,10 +294,10 @@ def run_gpu(args, rank, world, device):
         raise RuntimeError("pipelined end-to-end result differs from the device-resident run")
     del h_imgs, h_backs, d_imgs, sinos, backs
 
-    return dict(total=total, t_fwd=t_fwd, t_bwd=t_bwd, clocks=clocks, e2e_total=e2e_piped,
+    return dict(total=total, t_fwd=t_fwd, t_bwd=t_bwd, clocks=clocks, e2e_piped=e2e_piped,
                 e2e_serial=e2e_serial, e2e_buffers=nbuf,
                 h2d=h_img.numel() * 4, d2h=h_back.numel() * 4, ps=ps, tuned=tuned, flush=flush,
-                img=img)
+                img=img, sino=sino, back=back)
 
 
 def l1_load_peak(device, reps=5):
@@ -347,8 +351,11 @@ def extra_radon256(device, flush):
 
     res = {}
     host = random_ellipse_image(SEED, (256, 256), count=10, dtype="float64").T
+    cfg = dict(RADON_WORKLOAD)
+    cfg.pop("geometry")
+    shape, angles = cfg.pop("img_shape"), cfg.pop("angles")
     for name, tdt in (("float32", torch.float32), ("float64", torch.float64)):
-        ps = gg.ProjectionSettings(device, gg.RADON, (256, 256), 180, n_detectors=363)
+        ps = gg.ProjectionSettings(device, gg.RADON, shape, angles, **cfg)
         img = gg.core.empty((256, 256), tdt, "F", device)
         img.copy_(torch.from_numpy(np.ascontiguousarray(host.T)).T)
         sino = gg.core.empty(ps.sinogram_shape, tdt, "F", device)
@@ -361,7 +368,8 @@ def extra_radon256(device, flush):
         _event_times(step, 3, flush)
         t = _event_times(step, 50, flush)
         res[name] = 2 * 256 * 256 * 180 / statistics.median(t) / 1e9
-    return {"workload": "radon 256x256, 180 angles [0,pi), 363 detectors, fwd+back, L2 flushed",
+    return {"workload": "radon 256x256, 180 angles [0,pi), 363 detectors (width 2 sqrt 2), "
+                        "image width 2, fwd+back, L2 flushed",
             "unit": UNIT, **res}
 
 
@@ -378,12 +386,18 @@ def extra_cg50(device, ps, img):
     run = lambda: gg.conjugate_gradients(sino, ps, 50)  # noqa: E731
     _event_times(run, 2)
     t = _event_times(run, 5)
+    # error against a float64 solve of the same data: the float64 kernels
+    # (reference operation order, pinned to the float64 oracle at 1e-12)
+    out = run().double()
+    ref = gg.conjugate_gradients(sino.double(), ps, 50)
+    err = float(torch.linalg.norm(out - ref) / torch.linalg.norm(ref))
     return {"workload": "fanbeam 512x512, 360 angles, 768 detectors, 50 CG iterations, "
                         "1% Gaussian noise", "recon_per_s": 1.0 / statistics.median(t),
-            "ms_per_recon": statistics.median(t) * 1e3}
+            "ms_per_recon": statistics.median(t) * 1e3, "rel_err_vs_fp64": err,
+            "fp64_reference": "float64 CG on the same sinogram through the float64 kernels"}
 
 
-def extra_batched(device, small=False):
+def extra_batched(device, small=False, fp64_every=4):
     """Heterogeneous batch of 64 problems: batched persistent launches against per-call."""
     import torch
 
@@ -422,6 +436,18 @@ def extra_batched(device, small=False):
     for p, a, b in zip(solved, out_b, ref):
         e = float(torch.linalg.norm((a - b).double()) / torch.linalg.norm(b.double()))
         err[p.solver] = max(err.get(p.solver, 0.0), e)
+    # error against float64 solves of the same data (float64 kernels, the
+    # batch's norm estimates) for every fp64_every-th problem: float64
+    # projections run ~30x slower than float32 ones
+    err64, t64 = {}, time.perf_counter()
+    for k in range(0, len(solved), fp64_every):
+        p = solved[k]
+        q = gb.Problem(p.settings, p.sino.double(), p.solver, p.iterations, mu=p.mu,
+                       norm_estimate=p.norm_estimate)
+        b = gb.solve_plain([q])[0]
+        e = float(torch.linalg.norm(out_b[k].double() - b) / torch.linalg.norm(b))
+        err64[p.solver] = max(err64.get(p.solver, 0.0), e)
+    t64 = time.perf_counter() - t64
     name = ("64 problems, side U{32..128}, angles U[30,180]" if small else
             "64 problems, side U{128,192,256,384,512}, angles U[60,720]")
     return {"workload": name + ", half Radon (full or 2pi/3 range) half fan beam, "
@@ -429,6 +455,10 @@ def extra_batched(device, small=False):
             "batched_recon_per_s": 64 / t_b, "plain_graph_recon_per_s": 64 / t_pg,
             "plain_direct_recon_per_s": 64 / t_pd, "speedup_vs_plain_direct": t_pd / t_b,
             "speedup_vs_plain_graph": t_pg / t_b, "max_rel_err_vs_per_call": err,
+            "max_rel_err_vs_fp64": err64,
+            "fp64_reference": f"float64 per-call solves of every {fp64_every}th problem "
+                              f"({len(range(0, len(solved), fp64_every))} of {len(solved)}) "
+                              f"with the batch's norm estimates, {t64:.1f} s",
             "timing": "wall clock around the whole solve, synchronised"}
 
 
@@ -559,8 +589,15 @@ def launches_per_step(ps):
     return 4 if ps.img_shape[0] % 2 == 0 else 3
 
 
-def cpu_baseline_sample(max_seconds=12.0):
-    """Time the oracle (restated reference kernels) on this host's cores."""
+def cpu_baseline_sample(max_seconds=12.0, gpu_outputs=None):
+    """Time the oracle (restated reference kernels) on this host's cores.
+
+    With ``gpu_outputs = (sino, back)`` -- the GPU's float32 forward
+    projection of the workload image and the backprojection of that
+    sinogram, from the timed run -- the same leg also checks them against
+    the float64 oracle: forward against A x, backprojection against
+    A*(A x), relative L2 errors (the parity tests' bound is 1e-5).
+    """
     from oracle import oracle as O
     from tests.helpers import host_settings
 
@@ -576,8 +613,70 @@ def cpu_baseline_sample(max_seconds=12.0):
             break
     dt = time.perf_counter() - t0
     value = 2 * pixel_angles() * reps / dt / 1e9
-    return {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
-            "sample": f"{reps} forward+back steps of the full workload, {dt:.1f} s wall"}
+    out = {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
+           "sample": f"{reps} forward+back steps of the full workload, {dt:.1f} s wall"}
+    if gpu_outputs is not None:
+        g_sino, g_back = gpu_outputs
+        ref_sino = O.forward(np.asfortranarray(img, dtype=np.float64), ps)
+        ref_back = O.backward(np.asfortranarray(g_sino, dtype=np.float64), ps)
+
+        def rel(a, b):
+            return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+        out["parity"] = {"fwd_rel_err_vs_fp64_oracle": rel(g_sino, ref_sino),
+                         "bwd_rel_err_vs_fp64_oracle": rel(g_back, ref_back),
+                         "tolerance": 1e-5,
+                         "what": "the timed run's float32 outputs against the float64 oracle on "
+                                 "the same inputs (backprojection of the GPU sinogram)"}
+    return out
+
+
+def reference_arm(args):
+    """The oracle -- the C restatement of gratopy's OpenCL kernels, the reference's
+    own kernels needing an OpenCL runtime this machine lacks -- on all host
+    cores: ``warmup`` untimed and ``steps`` timed steps of forward + back.
+
+    A step projects the whole workload; when ``steps`` full steps would take
+    longer than about two minutes, every step projects an evenly spaced
+    subset of the angles instead (the same image and detector), and the
+    metric counts the pixel-angles actually processed.
+    """
+    from oracle import oracle as O
+    from tests.helpers import host_settings
+
+    ps = host_settings(WORKLOAD)
+    img = make_image()
+    Nx, Ny = WORKLOAD["img_shape"]
+
+    def step(p):
+        O.backward(O.forward(img, p), p)
+
+    t0 = time.perf_counter()
+    step(ps)  # also loads the library
+    t_full = time.perf_counter() - t0
+    stride = max(1, int(np.ceil(t_full * args.steps / 120.0)))
+    sample = ps
+    if stride > 1:
+        sample = host_settings(dict(WORKLOAD, angles=np.asarray(ps.angles)[::stride]))
+    for _ in range(args.warmup):
+        step(sample)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step(sample)
+    dt = time.perf_counter() - t0
+    units = 2 * Nx * Ny * sample.n_angles
+    value = units * args.steps / dt / 1e9
+    desc = ("the full workload" if stride == 1 else
+            f"{sample.n_angles} of the 360 angles (every {stride}th)")
+    base = {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
+            "sample": f"{args.steps} timed forward+back steps of {desc}, {dt:.1f} s wall"}
+    return {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded random ellipses",
+            "config": config_block(), "cpu_baseline": base,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
 
 
 def main():
@@ -605,17 +704,8 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        steps = max(1, args.steps)
-        base = cpu_baseline_sample(max_seconds=min(60.0, 3.0 * steps))
-        line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "impl": "reference",
-                "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
-                "ms_per_step": 2 * pixel_angles() / base["value"] / 1e6,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32", "data": "synthetic: seeded random ellipses",
-                "config": config_block(), "cpu_baseline": base,
-                "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        args.steps = max(1, args.steps)
+        print(json.dumps(reference_arm(args)))
         return
 
     import torch
@@ -629,7 +719,7 @@ def main():
     steps = args.steps
     units = 2 * pixel_angles() * world
     value = units * steps / res["total"] / 1e9
-    e2e = 2 * pixel_angles() * world * steps / res["e2e_total"] / 1e9
+    e2e_piped = 2 * pixel_angles() * world * steps / res["e2e_piped"] / 1e9
     e2e_serial = 2 * pixel_angles() * world * steps / res["e2e_serial"] / 1e9
     if rank != 0:
         if world > 1:
@@ -647,9 +737,8 @@ def main():
     fwd_name = "fan_fwd_quarter" if quarter else "fan_fwd_fast"
     bwd_name = "fan_bwd_orbit" if quarter and Nx % 2 == 0 else "fan_bwd_fast"
     dom, t_dom = (fwd_name, fwd) if fwd >= bwd else (bwd_name, bwd)
-    achieved = compulsory / t_dom / 1e9
     # DRAM traffic and issue utilisation of the dominant kernel from the
-    # committed ncu summary of this workload (not measured in this run)
+    # committed ncu summary of this workload (one capture, not this run)
     traffic, issue = None, None
     km_file = ROOT / "profiles" / "kernel_metrics.json"
     if km_file.exists():
@@ -659,40 +748,51 @@ def main():
             issue = km.get("issue_active_pct")
         except (OSError, ValueError):
             pass
+    # The projections are sparse gathers bound by L1 load throughput and
+    # instruction issue, not by HBM: the roofline divides the algorithmic
+    # gather bytes (2 nonzero weights x 4 B per pixel-angle) by the measured
+    # L1 load rate; the HBM figures (compulsory bytes: one read of the input,
+    # one write of the output) are kept beside it.
+    l1 = l1_load_peak(device)
+    gather_bytes = 8 * pixel_angles()
+    gather = gather_bytes / t_dom / 1e9
+    hbm_achieved = compulsory / t_dom / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": res["total"] / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded random ellipses (10 per image)",
-        "config": dict(config_block(), parallelism=f"replicas{world}"),
+        "config": config_block(),
+        "parallelism": f"replicas{world}",
         "fwd_gpixel_angle_per_s": pixel_angles() / fwd / 1e9,
         "bwd_gpixel_angle_per_s": pixel_angles() / bwd / 1e9,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-                     "algorithmic_bytes": compulsory, "peak_source": hbm_kind,
-                     "gather_bytes_per_s": 8 * pixel_angles() / t_dom / 1e9,
+        "roofline": {"bound": "l1", "kernel": dom, "achieved": gather, "peak": l1,
+                     "unit": "GB/s", "frac": gather / l1, "traffic": traffic,
+                     "algorithmic_bytes": gather_bytes,
+                     "peak_source": "measured in this run: gr_probe_l1_bandwidth (float4 loads "
+                                    "of an L1-resident buffer, every SM)",
+                     "hbm": {"achieved": hbm_achieved, "peak": hbm, "frac": hbm_achieved / hbm,
+                             "algorithmic_bytes": compulsory,
+                             "peak_source": f"{hbm_kind}: MEASURED_PEAKS.json hbm_gbs"},
                      "issue_active_pct_ncu": issue,
-                     "note": "issue- and L1-bound gather: compulsory HBM bytes are 2.15 MB per "
-                             "projection; the timed projection includes its orbit-copy "
-                             "pre-pass (one small kernel)"},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
+                     "traffic_source": "ncu capture of this workload (profiles/kernel_metrics.json)",
+                     "note": "the timed forward includes its orbit-copy pre-pass (one small "
+                             "kernel); DRAM traffic is the compulsory bytes plus the copy"},
+        "e2e": {"value": e2e_serial, "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"],
-                "mode": "public API, image uploaded from pinned host memory and backprojection "
-                        "read back every step; steps alternate between two streams so one "
-                        "step's copies overlap the other's projections; inputs rotate through "
-                        f"{res['e2e_buffers']} buffers (more than twice the L2), no flush",
-                "serial_value": e2e_serial,
-                "serial_mode": "one stream, L2 flushed before every step (outside the events)"},
+                "mode": "public API, one stream: the image uploaded from pinned host memory, "
+                        "forward + backprojection, the backprojection read back into pinned "
+                        "host memory, every step; L2 flushed before every step (outside the "
+                        "events)",
+                "pipelined_value": e2e_piped,
+                "pipelined_mode": "the same steps alternating between two streams, so one "
+                                  "step's copies overlap the other's projections; inputs rotate "
+                                  f"through {res['e2e_buffers']} buffers (more than twice the "
+                                  "L2), no flush"},
         "gpu_launches": launches_per_step(ps) * steps,
         "clocks": res["clocks"],
     }
     line["tuned_splits"] = res["tuned"]
-    # gather roofline: 8 B per pixel-angle against the measured L1 load rate
-    l1 = l1_load_peak(device)
-    gather = line["roofline"]["gather_bytes_per_s"]
-    line["roofline"]["l1"] = {"gather_gbs": gather, "peak_gbs": l1, "frac": gather / l1,
-                              "peak_source": "measured: gr_probe_l1_bandwidth (float4 loads, "
-                                             "L1-resident buffer)"}
     wanted = [] if args.no_extras else (
         DEFAULT_EXTRAS if args.extras == "all" else [e for e in args.extras.split(",") if e])
     for name in wanted:
@@ -700,7 +800,9 @@ def main():
             raise SystemExit(f"unknown extra workload {name!r}; choose from {', '.join(EXTRAS)}")
         line[name] = EXTRAS[name](device, ps, res)
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample()
+        outs = (res["sino"].cpu().numpy(), res["back"].cpu().numpy())
+        line["cpu_baseline"] = cpu_baseline_sample(gpu_outputs=outs)
+        line["parity"] = line["cpu_baseline"].pop("parity")
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

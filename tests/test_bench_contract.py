@@ -1,4 +1,4 @@
-"""bench.py's reference arm prints one JSON line with the contract's keys (CPU only)."""
+"""bench.py's workloads and its reference arm's JSON line (CPU only)."""
 
 from __future__ import annotations
 
@@ -7,7 +7,28 @@ import subprocess
 import sys
 from pathlib import Path
 
+import numpy as np
+import pytest
+
 ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT / "tests" / "golden"))
+import configs  # noqa: E402
+
+import bench  # noqa: E402
+
+
+@pytest.mark.parametrize("name,workload", [("bench_fan512", bench.WORKLOAD),
+                                           ("bench_radon256", bench.RADON_WORKLOAD)])
+def test_bench_workloads_match_fixture_table(name, workload):
+    """The bench's geometries are the fixture table's entries that the GPU parity
+    tests use (Radon: 363 detectors spanning the image diagonal, 2 sqrt 2)."""
+    want = configs.configs()[name]
+    assert workload.keys() == want.keys()
+    for k in want:
+        if isinstance(want[k], str):
+            assert workload[k] == want[k], k
+        else:
+            assert np.allclose(workload[k], want[k], rtol=1e-15, atol=0), k
 
 
 def test_reference_arm_json_line():

@@ -113,3 +113,45 @@ def test_heterogeneous_generator_runs(cuda_device):
     for x, pr in zip(out, problems):
         assert tuple(x.shape) == tuple(pr.settings.img_shape)
         assert torch.isfinite(x).all()
+
+
+def test_batched_against_fp64_oracle(cuda_device):
+    """Every problem of a heterogeneous batch against the float64 oracle's
+    solver on the same sinogram and norm estimate (gratopy.py:2380-2762).
+
+    Bound: max(1e-5, 3 x the float32 oracle's own distance from the float64
+    oracle) -- the solver bound of tests/test_gpu_solvers.py; the reported
+    error of each problem is its distance from float64.
+    """
+    from gratopy_gb300 import batch as gb
+    from oracle import oracle as O
+    from tests.helpers import HostSettings
+
+    problems = _problems(cuda_device)
+    results = gb.BatchedReconstruction(problems, cuda_device, normest_iterations=20).run()
+    for pr, got in zip(problems, results):
+        ps = pr.settings
+        hps = HostSettings(ps.geometry, ps.img_shape, np.asarray(ps.angles),
+                           n_detectors=ps.n_detectors, angle_weights=np.asarray(ps.angle_weights),
+                           detector_width=ps.detector_width, image_width=ps.image_width,
+                           R=ps.R, RE=ps.RE, detector_shift=ps.detector_shift,
+                           midpoint_shift=ps.midpoint_shift,
+                           reverse_detector=ps.reverse_detector)
+        f32 = np.asfortranarray(pr.sino.cpu().numpy())
+        outs = []
+        for f in (np.asfortranarray(f32, np.float64), f32):
+            if pr.solver == "landweber":
+                outs.append(O.landweber(f, hps, pr.iterations, w=pr.w,
+                                        norm_estimate=pr.norm_estimate))
+            elif pr.solver == "cg":
+                outs.append(O.conjugate_gradients(f, hps, pr.iterations))
+            else:
+                outs.append(O.total_variation(f, hps, pr.mu, pr.iterations,
+                                              stepsize_weighting=pr.stepsize_weighting,
+                                              norm_estimate=pr.norm_estimate))
+        ref64, ref32 = outs
+        err = rel_l2(got.cpu().numpy(), ref64)
+        base = rel_l2(ref32, ref64)
+        assert err <= max(1e-5, 3.0 * base), (
+            f"{pr.solver} {ps.geometry} {ps.img_shape}: rel err vs float64 {err:.3e} "
+            f"(float32 oracle {base:.3e})")
