@@ -76,6 +76,7 @@ SIGNATURES = {
     "gr_error_string": (ctypes.c_char_p, [_I]),
     "gr_last_cuda_error": (_I, []),
     "gr_version": (_I, []),
+    "gr_source_hash": (ctypes.c_char_p, []),
     "gr_radon_fwd": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "gr_radon_bwd": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "gr_fan_fwd": (_I, [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
@@ -144,6 +145,13 @@ def load():
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        from .build import source_hash
+
+        built, current = lib.gr_source_hash().decode(), source_hash()
+        if built != current:
+            raise ImportError(
+                f"{LIB_PATH} was built from other sources (library {built[:16]}, sources "
+                f"{current[:16]}); rebuild with `python -m gratopy_gb300.build`")
         _lib = lib
     return _lib
 

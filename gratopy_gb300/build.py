@@ -8,6 +8,7 @@ The library exports the C ABI declared in ``include/gratopy_gb300.h``.
 
 from __future__ import annotations
 
+import hashlib
 import os
 import shutil
 import subprocess
@@ -48,11 +49,28 @@ def _deps() -> list[Path]:
     return sources() + sorted(CSRC.glob("*.cuh")) + [INCLUDE / "gratopy_gb300.h", Path(__file__)]
 
 
-def needs_build() -> bool:
+def source_hash() -> str:
+    """Hex SHA-256 over the names and contents of every input of the build;
+    compiled into the library (``gr_source_hash``) and compared at load."""
+    h = hashlib.sha256()
+    for p in _deps():
+        h.update(p.name.encode() + b"\0" + p.read_bytes() + b"\0")
+    return h.hexdigest()
+
+
+def _built_hash() -> str | None:
+    """``gr_source_hash`` of the library on disk, read in a subprocess so
+    this process does not keep an outdated library mapped."""
     if not LIB.exists():
-        return True
-    mtime = LIB.stat().st_mtime
-    return any(p.stat().st_mtime > mtime for p in _deps())
+        return None
+    code = ("import ctypes,sys; f=ctypes.CDLL(sys.argv[1]).gr_source_hash; "
+            "f.restype=ctypes.c_char_p; print(f().decode())")
+    res = subprocess.run([sys.executable, "-c", code, str(LIB)], capture_output=True, text=True)
+    return res.stdout.strip() if res.returncode == 0 else None
+
+
+def needs_build() -> bool:
+    return _built_hash() != source_hash()
 
 
 def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
@@ -60,7 +78,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
         return LIB
     OUT_DIR.mkdir(exist_ok=True)
     cc = nvcc()
-    flags = NVCC_FLAGS + (extra_flags or [])
+    flags = NVCC_FLAGS + [f'-DGR_SOURCE_HASH="{source_hash()}"'] + (extra_flags or [])
 
     def compile_one(src: Path) -> Path:
         obj = OUT_DIR / (src.stem + ".o")

@@ -21,9 +21,12 @@ namespace {
 constexpr size_t kMaxPartials = 65536;
 __device__ __align__(256) double g_wsq_partials[kMaxPartials];
 
-// Device address of g_wsq_partials, looked up once per device.  In host code
-// the symbol name is only a host-side stand-in, so kernels are always given
-// this looked-up address.
+// Device address of g_wsq_partials, looked up once per device and kept for
+// the life of the process.  In host code the symbol name is only a host-side
+// stand-in, so kernels are always given this looked-up address.  A
+// cudaDeviceReset destroys the context the address belongs to, and the kept
+// address is not looked up again: this entry point must not be called on a
+// device after a reset of that device.
 constexpr int kMaxDevices = 64;
 double* g_partials_addr[kMaxDevices] = {nullptr};
 std::mutex g_setup_mutex;
@@ -59,6 +62,10 @@ int gr_forward_wsq_noalloc(const gr_geometry* g, void* q, const void* p, const v
   if (g == nullptr || q == nullptr || p == nullptr || w == nullptr || out == nullptr ||
       !gr::valid_order(order) || !gr::valid_dtype(g->dtype))
     return GR_ERR_ARG;
+  // sizes first: the partial count below is only meaningful for a valid geometry
+  const int geo_rc = gr::launch::check_geometry(g);
+  if (geo_rc != GR_OK) return geo_rc;
+  if (Nz <= 0) return GR_ERR_SHAPE;
   const size_t n = gr_forward_partials(g, Nz);
   if (n == 0) return GR_ERR_ARG;
   if (n > kMaxPartials) return GR_ERR_TOO_BIG;

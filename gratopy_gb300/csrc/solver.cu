@@ -208,6 +208,11 @@ int gr_last_cuda_error(void) { return gr::g_last_cuda_error; }
 
 int gr_version(void) { return 1; }
 
+#ifndef GR_SOURCE_HASH
+#define GR_SOURCE_HASH "unknown"
+#endif
+const char* gr_source_hash(void) { return GR_SOURCE_HASH; }
+
 int gr_weight_sinogram(void* out, const void* sino, const void* w, int dtype, int Ns, int Na,
                        int Nz, int order, int divide, void* stream) {
   if (!out || !sino || !w || !valid_dtype(dtype) || !valid_order(order)) return GR_ERR_ARG;

@@ -63,7 +63,9 @@ class _CUDAOperator(Operator):
             array = np.ascontiguousarray(array)
         if array.flags["C_CONTIGUOUS"]:
             return torch.from_numpy(array).to(device)
-        return torch.from_numpy(array.T.copy()).to(device).T
+        # Fortran order: upload the reversed-axes C array, view it back
+        axes = tuple(reversed(range(array.ndim)))
+        return torch.from_numpy(np.ascontiguousarray(array.transpose(axes))).to(device).permute(axes)
 
     @staticmethod
     def _default_order(reference: torch.Tensor) -> str:

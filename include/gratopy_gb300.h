@@ -93,6 +93,10 @@ GR_API size_t gr_geometry_size(void);
 /* Last CUDA error seen by this library on the calling thread (cudaError_t). */
 GR_API int gr_last_cuda_error(void);
 GR_API int gr_version(void);
+/* Hex SHA-256 of the sources this library was compiled from (csrc/*.cu,
+ * csrc/*.cuh, this header and the build recipe), so a binding can refuse a
+ * library left over from other sources. */
+GR_API const char* gr_source_hash(void);
 
 /* ---- The four projection kernels, argument order as gratopy's kernels ----
  * radon.cl:66-161    radon_{T}_{so}{io}(sino, img, ofs, Geometryinformation) */
@@ -152,8 +156,12 @@ GR_API int gr_backward_cg(const gr_geometry* g, void* snew, const void* d, void*
  * (gr_forward_partials(g, Nz) <= 65536, else GR_ERR_TOO_BIG); 512 KiB is
  * held on every GPU that loads the library until exit.  The first call on
  * each device looks that array's address up (cudaGetSymbolAddress), so make
- * it before any stream capture.  All calls share the array: calls that
- * overlap on the GPU race. */
+ * it before any stream capture; the address is kept for the life of the
+ * process, so after a cudaDeviceReset of a device this entry point must not
+ * be called on that device again.  All calls share the array: calls that
+ * overlap on the GPU (several streams, several host threads) race, so the
+ * caller serialises them, for example on one stream.  Invalid sizes return
+ * GR_ERR_SHAPE before the partial count is checked. */
 GR_API int gr_forward_wsq_noalloc(const gr_geometry* g, void* q, const void* p, const void* w,
                                   double* out, int Nz, int order, void* stream);
 /* Transposes for differentiation (no counterpart in the reference, which

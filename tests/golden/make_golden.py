@@ -1,9 +1,10 @@
 """Generate the golden fixtures of tests/golden/ from the gratopy reference.
 
-Run on a machine that has the reference checked out at /root/reference
-(the tests only read the committed outputs and never run this):
+Run on a machine that has a checkout of the gratopy reference, giving its
+root directory (the tests only read the committed outputs and never run
+this):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py PATH/TO/gratopy-checkout
 
 It imports gratopy's pure-NumPy host code (``pyopencl`` and ``matplotlib``
 are stubbed -- no OpenCL runtime is needed for geometry tables) and writes:
@@ -44,7 +45,7 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path("/root/reference")
+REF = Path(".")  # root of the gratopy checkout; set from the command line by main()
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
 import configs as cfgmod  # noqa: E402
@@ -213,4 +214,11 @@ def main():
 
 
 if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser(description="regenerate tests/golden from a gratopy checkout")
+    ap.add_argument("reference", type=Path, help="root directory of the gratopy checkout")
+    REF = ap.parse_args().reference.resolve()
+    if not (REF / "gratopy" / "gratopy.py").exists():
+        raise SystemExit(f"{REF} is not a gratopy checkout (gratopy/gratopy.py missing)")
     main()

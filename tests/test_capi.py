@@ -53,6 +53,9 @@ def test_host_only_entry_points(library):
 
     lib = _lib.load()
     assert lib.gr_version() == 1
+    from gratopy_gb300 import build
+
+    assert lib.gr_source_hash().decode() == build.source_hash()
     assert lib.gr_error_string(0) == b"success"
     assert b"geometry" in lib.gr_error_string(1)
     assert lib.gr_dot_partials_count() > 0

@@ -119,9 +119,13 @@ def test_batched_against_fp64_oracle(cuda_device):
     """Every problem of a heterogeneous batch against the float64 oracle's
     solver on the same sinogram and norm estimate (gratopy.py:2380-2762).
 
-    Bound: max(1e-5, 3 x the float32 oracle's own distance from the float64
-    oracle) -- the solver bound of tests/test_gpu_solvers.py; the reported
-    error of each problem is its distance from float64.
+    Bound: max(1e-5, 3 x the float32 envelope), the envelope being the
+    largest distance from the float64 result among float32 runs of the
+    reference's arithmetic (the float32 oracle on the sinogram and on three
+    copies perturbed by one unit in the last place).  Landweber and TV keep
+    float32 runs within ~1e-7 of float64; CG amplifies rounding (its
+    iterates lose orthogonality) and equally valid float32 runs land ~1e-4
+    apart on these noisy problems.
     """
     from gratopy_gb300 import batch as gb
     from oracle import oracle as O
@@ -138,8 +142,11 @@ def test_batched_against_fp64_oracle(cuda_device):
                            midpoint_shift=ps.midpoint_shift,
                            reverse_detector=ps.reverse_detector)
         f32 = np.asfortranarray(pr.sino.cpu().numpy())
+        rng = np.random.default_rng(0)
+        perturbed = [np.asfortranarray((f32 * (1 + 2.0**-24 * rng.standard_normal(f32.shape)))
+                                       .astype(np.float32)) for _ in range(3)]
         outs = []
-        for f in (np.asfortranarray(f32, np.float64), f32):
+        for f in [np.asfortranarray(f32, np.float64), f32] + perturbed:
             if pr.solver == "landweber":
                 outs.append(O.landweber(f, hps, pr.iterations, w=pr.w,
                                         norm_estimate=pr.norm_estimate))
@@ -149,9 +156,9 @@ def test_batched_against_fp64_oracle(cuda_device):
                 outs.append(O.total_variation(f, hps, pr.mu, pr.iterations,
                                               stepsize_weighting=pr.stepsize_weighting,
                                               norm_estimate=pr.norm_estimate))
-        ref64, ref32 = outs
+        ref64 = outs[0]
         err = rel_l2(got.cpu().numpy(), ref64)
-        base = rel_l2(ref32, ref64)
-        assert err <= max(1e-5, 3.0 * base), (
+        envelope = max(rel_l2(o, ref64) for o in outs[1:])
+        assert err <= max(1e-5, 3.0 * envelope), (
             f"{pr.solver} {ps.geometry} {ps.img_shape}: rel err vs float64 {err:.3e} "
-            f"(float32 oracle {base:.3e})")
+            f"(float32 envelope {envelope:.3e})")

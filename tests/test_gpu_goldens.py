@@ -3,9 +3,12 @@ utility functions against the oracle.
 
 Each golden is a control number hard-coded in gratopy's test-suite
 (file:line per test), pinned at gratopy's rtol 1e-3; the same outputs are
-also compared with the float64 oracle on the same inputs (relative L2 1e-5
-for the float32 kernels).  The oracle side of these cases is pinned to the
-same numbers on the CPU by tests/test_oracle_pins.py.
+also compared with the float64 oracle on the same inputs.  The float32
+bound is 1e-5 relative L2, or 1.25 x the error of the reference's own
+float32 arithmetic (the float32 oracle) where that is larger: on the
+strongly magnifying midpoint-shifted fan geometry (R = 5, RE = 3) the
+float32 oracle itself is 1.09e-5 from float64.  The oracle side of these
+cases is pinned to the same numbers on the CPU by tests/test_oracle_pins.py.
 """
 
 from __future__ import annotations
@@ -49,6 +52,26 @@ def _np(t):
     return t.detach().cpu().numpy()
 
 
+def _fwd_parity(gpu_sino, img, hps):
+    """Forward projection within max(1e-5, 1.25 x the float32 oracle's error)."""
+    ref = O.forward(np.asfortranarray(img, np.float64), hps)
+    err = rel_l2(gpu_sino, ref)
+    if err <= 1e-5:
+        return
+    own = rel_l2(O.forward(np.asfortranarray(img, np.float32), hps), ref)
+    assert err <= 1.25 * own, f"forward rel err {err:.3e} (float32 oracle {own:.3e})"
+
+
+def _bwd_parity(gpu_back, sino, hps):
+    """Backprojection of ``sino`` within max(1e-5, 1.25 x the float32 oracle's error)."""
+    ref = O.backward(np.asfortranarray(sino, np.float64), hps)
+    err = rel_l2(gpu_back, ref)
+    if err <= 1e-5:
+        return
+    own = rel_l2(O.backward(np.asfortranarray(sino, np.float32), hps), ref)
+    assert err <= 1.25 * own, f"backprojection rel err {err:.3e} (float32 oracle {own:.3e})"
+
+
 @pytest.fixture(scope="module")
 def phantoms1200():
     return create_phantoms(1200, "float32", "F")
@@ -81,10 +104,8 @@ def test_radon_limited_angles(cuda_device, phantoms1200):
     incorrect.set_angle_weights(correct.angle_weights)
     assert_control(_np(gg.backprojection(s_c, incorrect)), dims, 3385.137, "img", "back repaired")
     # the oracle on the same inputs
-    hps = host_settings(CFG["radon_limited_correct"])
-    assert rel_l2(_np(s_c), O.forward(np.asfortranarray(img, np.float64), hps)) <= 1e-5
-    assert rel_l2(_np(back_i), O.backward(np.asfortranarray(_np(s_c), np.float64),
-                                           host_settings(CFG["radon_limited_incorrect"]))) <= 1e-5
+    _fwd_parity(_np(s_c), img, host_settings(CFG["radon_limited_correct"]))
+    _bwd_parity(_np(back_i), _np(s_c), host_settings(CFG["radon_limited_incorrect"]))
 
 
 def test_fan_limited_angles(cuda_device, phantoms1200):
@@ -103,10 +124,8 @@ def test_fan_limited_angles(cuda_device, phantoms1200):
     assert_control(_np(gg.backprojection(s_c2, correct2)), dims, 19495.96, "img", "back correct2")
     back_i = gg.backprojection(s_c, incorrect)
     assert_control(_np(back_i), dims, 23043.191, "img", "back incorrect")
-    hps = host_settings(CFG["fan_limited_correct"])
-    assert rel_l2(_np(s_c), O.forward(np.asfortranarray(img, np.float64), hps)) <= 1e-5
-    assert rel_l2(_np(back_i), O.backward(np.asfortranarray(_np(s_c), np.float64),
-                                           host_settings(CFG["fan_limited_incorrect"]))) <= 1e-5
+    _fwd_parity(_np(s_c), img, host_settings(CFG["fan_limited_correct"]))
+    _bwd_parity(_np(back_i), _np(s_c), host_settings(CFG["fan_limited_incorrect"]))
 
 
 @pytest.mark.parametrize("name,golden", [
@@ -124,8 +143,8 @@ def test_nonquadratic(cuda_device, phantoms1200, name, golden):
     assert_control(_np(sino), dims, golden[1], "sino", "sinogram")
     assert_control(_np(back), dims, golden[2], "img", "backprojection")
     hps = host_settings(CFG[name])
-    assert rel_l2(_np(sino), O.forward(np.asfortranarray(img, np.float64), hps)) <= 1e-5
-    assert rel_l2(_np(back), O.backward(np.asfortranarray(_np(sino), np.float64), hps)) <= 1e-5
+    _fwd_parity(_np(sino), img, hps)
+    _bwd_parity(_np(back), _np(sino), hps)
 
 
 @pytest.mark.parametrize("name,golden", [
@@ -141,9 +160,8 @@ def test_midpoint_shift(cuda_device, phantoms1200, name, golden):
     assert_control(_np(sino), dims, golden[0], "sino", "sinogram")
     assert_control(_np(back), dims, golden[1], "img", "backprojection")
     hps = host_settings(CFG[name])
-    ref = O.forward(np.asfortranarray(phantoms1200, np.float64), hps)
-    assert rel_l2(_np(sino), ref) <= 1e-5
-    assert rel_l2(_np(back), O.backward(np.asfortranarray(_np(sino), np.float64), hps)) <= 1e-5
+    _fwd_parity(_np(sino), phantoms1200, hps)
+    _bwd_parity(_np(back), _np(sino), hps)
 
 
 ORIENTATION = [  # tests/test_fanbeam.py:769-943
@@ -174,8 +192,7 @@ def test_geometric_orientation(cuda_device, j):
         for m, img in enumerate((img1, img2)):
             sino = _np(gg.forwardprojection(_dev(img, cuda_device), ps))
             assert_control(sino, dims, golden[2 * k + m], "sino", f"{geom} image {m + 1}")
-            ref = O.forward(np.require(img, np.float64, "C"), hps)
-            assert rel_l2(sino, ref) <= 1e-5, geom
+            _fwd_parity(sino, img, hps)
 
 
 # ------------------------------------------------------- utility functions

@@ -237,9 +237,11 @@ def test_fanbeam_operator_parity(cuda_device, dtype, order, nz, symmetric):
 
 
 def test_operator_adjointness(cuda_device):
-    """<R x, y> = <x, R.T y> in the operators' own inner products: R.T is
-    gratopy's backprojection, the adjoint in the angle-weighted sinogram
-    inner product scaled by ds / dx^2 (float64, 1e-12)."""
+    """<R x, W y> ds = <x, R.T y> dx^2 (float64): R.T is gratopy's
+    backprojection, the adjoint of R in the angle-weighted sinogram inner
+    product.  It holds to 1e-6, not to float64 rounding: the Radon forward
+    scales by dx and ds rounded to float32 (radon.cl:82-83) in both
+    precisions, an offset of ~1e-8 relative."""
     import torch
 
     from gratopy_gb300.operator import Radon
@@ -253,4 +255,4 @@ def test_operator_adjointness(cuda_device):
     w = torch.as_tensor(np.asarray(ps.angle_weights), device=cuda_device, dtype=torch.float64)
     lhs = float((Rx * y * w[None, :]).sum()) * ps.delta_s
     rhs = float((x * R.T.apply_to(y)).sum()) * ps.delta_x ** 2
-    assert abs(lhs - rhs) <= 1e-12 * abs(rhs)
+    assert abs(lhs - rhs) <= 1e-6 * abs(rhs)
