@@ -165,9 +165,8 @@ inline bool use_quarter(const gr_geometry* g, int Nz) {
 // a quarter about the image centre and the others are its powers, the side
 // is even (the quadrant x, y < N/2 then holds one pixel of every orbit),
 // and a slice of the sinogram has fewer than 2^31 values (32-bit offsets).
-inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
-  if (!use_quarter(g, Nz) || g->Nx % 2 != 0) return false;
-  if ((int64_t)g->Ns * g->Na > INT32_MAX) return false;
+// The three maps are the powers of one quarter turn about the image centre.
+inline bool maps_cyclic(const gr_geometry* g) {
   const int* m1 = g->sym_map[0];
   if (m1[0] != 0 || m1[3] != 0 || m1[1] * m1[2] != -1) return false;
   // apply the first map after an affine map (axx, axy, ayx, ayy, cx, cy)
@@ -187,6 +186,12 @@ inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
   for (int k = 0; k < 6; ++k)
     if (m2[k] != g->sym_map[1][k] || m3[k] != g->sym_map[2][k] || m4[k] != id[k]) return false;
   return true;
+}
+
+inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
+  if (!use_quarter(g, Nz) || g->Nx % 2 != 0) return false;
+  if ((int64_t)g->Ns * g->Na > INT32_MAX) return false;
+  return maps_cyclic(g);
 }
 
 // Scratch of the orbit kernels: the forward's orbit pixels (one float4 per
@@ -210,7 +215,8 @@ inline size_t quarter_fwd_bytes(const gr_geometry* g, int Nz) {
 
 inline size_t quarter_bwd_bytes(const gr_geometry* g, int Nz) {
   if (!use_quarter_bwd(g, Nz) || pixel_angles(g) < kQuarterBwdCopyMin) return 0;
-  return (size_t)(g->Na / 4) * (size_t)g->Ns * sizeof(float4);
+  return (size_t)(g->Na / 4) * (size_t)(g->Ns + fast::kOrbitRowPad + fast::kOrbitRec) *
+         sizeof(float4);
 }
 
 inline size_t orbit_work_bytes(const gr_geometry* g, int Nz) {
@@ -250,6 +256,7 @@ inline fast::QuarterMaps quarter_maps(const gr_geometry* g) {
     q.cx[m] = g->sym_map[m][4];
     q.cy[m] = g->sym_map[m][5];
   }
+  q.cyclic = maps_cyclic(g) ? 1 : 0;
   return q;
 }
 
@@ -389,17 +396,17 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
         const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
         for (int z0 = 0; z0 < Nz; z0 += chunk) {
           const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;
-          const dim3 rgrid((g->Ns + 255) / 256, g->Na / 4, zc);
-          fast::orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, sdpd, d, rows4, z0, skip);
-          fast::fan_bwd_orbit<IO, SO, SPLIT, true, Epi>
-              <<<dim3(grid.x, grid.y, zc), block, 0, st>>>(
-                  sino, rows4, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi,
-                  partials ? partials + z0 * per_slice_blocks : nullptr, skip, z0);
+          // one more block column writes the base angles' records
+          const dim3 rgrid((g->Ns + fast::kOrbitRowPad + 255) / 256 + 1, g->Na / 4, zc);
+          fast::orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, sdpd, ofs, fan_geo<float>(g->geo), d,
+                                                      rows4, z0, skip);
+          fast::fan_bwd_orbit_rows<IO, SPLIT, Epi><<<dim3(grid.x, grid.y, zc), block, 0, st>>>(
+              rows4, fan_geo<float>(g->geo), d, quarter_maps(g), epi,
+              partials ? partials + z0 * per_slice_blocks : nullptr, skip, z0);
         }
       } else {
-        fast::fan_bwd_orbit<IO, SO, SPLIT, false, Epi><<<grid, block, 0, st>>>(
-            sino, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials,
-            skip, 0);
+        fast::fan_bwd_orbit<IO, SO, SPLIT, Epi><<<grid, block, 0, st>>>(
+            sino, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials, skip, 0);
       }
     } else if (g->kind == GR_RADON) {
       fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, fblock, 0, st>>>(

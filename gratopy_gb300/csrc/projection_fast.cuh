@@ -781,6 +781,10 @@ fan_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs,
 // angle a + m Na/4.
 struct QuarterMaps {
   int axx[3], axy[3], ayx[3], ayy[3], cx[3], cy[3];
+  // nonzero when map m is the m-th power of one quarter turn: then the
+  // relation holds from every angle of an orbit, not only from the base
+  // angles in [0, Na/4)
+  int cyclic;
 };
 
 // img (and img4) point at slice z; offsets within a slice are 32-bit except
@@ -799,22 +803,47 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
   const int64_t a = bid.y;              // base angle in [0, Na/4)
   const int64_t quarter = d.Na / kOrbit;
   const bool active = s0 < d.Ns;
-  float acc[kOrbit][kRayGroup];
+  // bin q's sums for the orbit angles (0, 1) and (2, 3): one register pair
+  // each, updated by packed float32 multiply-adds (two lanes per instruction)
+  float2 acc01[kRayGroup], acc23[kRayGroup];
 #pragma unroll
-  for (int m = 0; m < kOrbit; ++m)
-#pragma unroll
-    for (int q = 0; q < kRayGroup; ++q) acc[m][q] = 0.0f;
+  for (int q = 0; q < kRayGroup; ++q) acc01[q] = acc23[q] = make_float2(0.0f, 0.0f);
   const float R = g.R;
+  int shift = 0;  // accumulator m belongs to row a + ((m + shift) mod 4) Na/4
   if (active) {
     float midx = g.midx, midy = g.midy;
-    const float* o = ofs + 8 * a;
-    float dx = o[0], dy = o[1], qx = o[2], qy = o[3];
-    const float d0x = o[4], d0y = o[5];
     const float sr = (float)(int)s0;
     const float fp = -g.mid_det + sr + (float)kRayGroup;
     const float fm = -g.mid_det + sr - 1.0f;
-    float dpx = d0x + dx * fp - qx, dpy = d0y + dy * fp - qy;
-    float dmx = d0x + dx * fm - qx, dmy = d0y + dy * fm - qy;
+    // rays through the group's outer bins -1 and kRayGroup at angle `ang`
+    auto boundary_rays = [&](int64_t ang, float& px, float& py, float& mx, float& my) {
+      const float* q = ofs + 8 * ang;
+      px = q[4] + q[0] * fp - q[2];
+      py = q[5] + q[1] * fp - q[3];
+      mx = q[4] + q[0] * fm - q[2];
+      my = q[5] + q[1] * fm - q[3];
+    };
+    int64_t ab = a;  // the orbit angle whose geometry this group walks
+    {
+      float px, py, mx, my;
+      boundary_rays(a, px, py, mx, my);
+      // With cyclic maps every member of the orbit can serve as the base.
+      // Walk a + Na/4 (rays turned by a quarter) when a's rays through this
+      // group are steep: the group's lanes then take adjacent image columns
+      // and walk down them, so one load instruction of a group reads
+      // adjacent pixels (measured at 512^2 x 360: 1181 Gpixel-angle/s with
+      // every group in this orientation, 1045 with every group walking
+      // rows, 1152 with the orientation of the base angle a alone).
+      if (qm.cyclic && fabsf(px) < fabsf(py) && fabsf(mx) < fabsf(my)) {
+        ab = a + quarter;
+        shift = 1;
+      }
+    }
+    const float* o = ofs + 8 * ab;
+    float dx = o[0], dy = o[1], qx = o[2], qy = o[3];
+    const float d0x = o[4], d0y = o[5];
+    float dpx, dpy, dmx, dmy;
+    boundary_rays(ab, dpx, dpy, dmx, dmy);
     float ddx = (d0x - qx) / (R * R), ddy = (d0y - qy) / (R * R);
     const float xx2 = g.delta_xi * g.delta_xi;
     dx /= xx2;
@@ -885,38 +914,69 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
 #pragma unroll
         for (int m = 0; m < kOrbit - 1; ++m) om[m] = mbase[m] + y * mstep_y[m] + xlo * mstep_x[m];
       }
+      if constexpr (PIX4) {
+        // two candidates per trip, both loads in flight (one per trip
+        // measured 1115 instead of 1181 Gpixel-angle/s at 512^2 x 360); the
+        // second of an odd count is masked (its reciprocal set to zero adds
+        // zeros).  t and ss advance by the same additions as one candidate
+        // per trip.
+        for (int x = xlo; x <= xhi; x += 2) {
+          const bool two = x < xhi;
+          const float tb = t + ddx, sb = ss + dx;
+          const float4 pa = __ldg(img4 + o0);
+          const float4 pb = __ldg(img4 + (two ? o0 + stp : o0));
+          const float ra = rcp_approx(t);
+          const float rb = two ? rcp_approx(tb) : 0.0f;
+          const float ua = fmaf(ss, ra, -s_mid0), ub = fmaf(sb, rb, -s_mid0);
+          const float2 ra2 = make_float2(ra, ra), rb2 = make_float2(rb, rb);
+          const float2 a01 = __fmul2_rn(make_float2(pa.x, pa.y), ra2);
+          const float2 a23 = __fmul2_rn(make_float2(pa.z, pa.w), ra2);
+          const float2 b01 = __fmul2_rn(make_float2(pb.x, pb.y), rb2);
+          const float2 b23 = __fmul2_rn(make_float2(pb.z, pb.w), rb2);
+#pragma unroll
+          for (int q = 0; q < kRayGroup; ++q) {
+            const float wa = fmaxf(0.0f, 1.0f - fabsf((float)q - ua));
+            const float wb = fmaxf(0.0f, 1.0f - fabsf((float)q - ub));
+            const float2 wa2 = make_float2(wa, wa), wb2 = make_float2(wb, wb);
+            acc01[q] = __ffma2_rn(wb2, b01, __ffma2_rn(wa2, a01, acc01[q]));
+            acc23[q] = __ffma2_rn(wb2, b23, __ffma2_rn(wa2, a23, acc23[q]));
+          }
+          o0 += 2 * stp;
+          t = tb + ddx;
+          ss = sb + dx;
+        }
+      } else {
       for (int x = xlo; x <= xhi; ++x) {
         const float r = rcp_approx(t);
         const float u = fmaf(ss, r, -s_mid0);
-        float v[kOrbit];
-        if constexpr (PIX4) {
-          const float4 p4 = __ldg(img4 + o0);
-          v[0] = p4.x * r;
-          v[1] = p4.y * r;
-          v[2] = p4.z * r;
-          v[3] = p4.w * r;
-        } else {
-          v[0] = ldg(img + o0) * r;
-#pragma unroll
-          for (int m = 0; m < kOrbit - 1; ++m) v[m + 1] = ldg(img + om[m]) * r;
-        }
+        const float2 r2 = make_float2(r, r);
+        const float2 v01 = __fmul2_rn(make_float2(ldg(img + o0), ldg(img + om[0])), r2);
+        const float2 v23 = __fmul2_rn(make_float2(ldg(img + om[1]), ldg(img + om[2])), r2);
+        // hat weights, zero outside a bin's pair of neighbouring rays: the
+        // multiply-add of a zero weight leaves the sum unchanged, so no branch
 #pragma unroll
         for (int q = 0; q < kRayGroup; ++q) {
-          const float w = 1.0f - fabsf((float)q - u);
-          if (w > 0.0f) {
-#pragma unroll
-            for (int m = 0; m < kOrbit; ++m) acc[m][q] = fmaf(w, v[m], acc[m][q]);
-          }
+          const float w = fmaxf(0.0f, 1.0f - fabsf((float)q - u));
+          const float2 w2 = make_float2(w, w);
+          acc01[q] = __ffma2_rn(w2, v01, acc01[q]);
+          acc23[q] = __ffma2_rn(w2, v23, acc23[q]);
         }
         o0 += stp;
-        if constexpr (!PIX4) {
 #pragma unroll
-          for (int m = 0; m < kOrbit - 1; ++m) om[m] += mstep_x[m];
-        }
+        for (int m = 0; m < kOrbit - 1; ++m) om[m] += mstep_x[m];
         t += ddx;
         ss += dx;
       }
+      }
     }
+  }
+  float acc[kOrbit][kRayGroup];
+#pragma unroll
+  for (int q = 0; q < kRayGroup; ++q) {
+    acc[0][q] = acc01[q].x;
+    acc[1][q] = acc01[q].y;
+    acc[2][q] = acc23[q].x;
+    acc[3][q] = acc23[q].y;
   }
   if (SPLIT > 1) {
 #pragma unroll
@@ -931,7 +991,7 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
         const float sc = sdpd[s] / g.delta_xi * g.delta_x / R;
 #pragma unroll
         for (int m = 0; m < kOrbit; ++m) {
-          const int64_t am = a + m * quarter;
+          const int64_t am = a + ((m + shift) & (kOrbit - 1)) * quarter;
           part += epi(s, am, z, sino_index<SO>(s, am, z, d), acc[m][q] * sc);
         }
       }
@@ -1011,26 +1071,71 @@ orbit_pixels_tiled(const float* __restrict__ img, Dims d, QuarterMaps qm,
 }
 
 // The four sinogram rows of every quarter-turn orbit of angles, premultiplied
-// by sdpd, as one float4 per (base angle, bin): rows4[a Ns + s] =
+// by sdpd, as one float4 per (base angle, bin), with one zero entry before
+// the detector and two after it: row a holds at 1 + s the float4
 // sdpd[s] (sino[s, a], sino[s, a + Q], sino[s, a + 2Q], sino[s, a + 3Q]),
-// Q = Na / 4.  Lanes run along the bins (coalesced for F-ordered sinograms);
-// slice z0 + blockIdx.z goes to copy blockIdx.z.
+// Q = Na / 4, so a backprojection that clamps its interpolation position to
+// [-1, Ns] reads zeros off the detector without testing the bins.  (Entries
+// holding both taps of a position, 32 bytes read by one load, measured
+// slower: twice the footprint, L1 hit rate 63% -> 22%.)  Lanes run along the
+// bins (coalesced for F-ordered sinograms); slice z0 + blockIdx.z goes to
+// copy blockIdx.z.
+constexpr int kOrbitRowPad = 3;  // entries per row: Ns + kOrbitRowPad
+constexpr int kOrbitRec = 4;     // float4 per base angle in the record table
+
+// Per-base-angle record of the orbit backprojection, as broadcast pairs for
+// the packed arithmetic: (ddx, ddx, ddy, ddy), (tz, tz, dx, dx),
+// (dy, dy, sz, sz), (w0, w1, w2, w3) with t = ddx X + ddy Y + tz and
+// s = dx X + dy Y + sz for pixel centres (X, Y) relative to the image
+// midpoint (source offset folded into tz and sz), and w_j the angle weight
+// of row a + j Q divided by R.
+__device__ __forceinline__ void orbit_record(float4* __restrict__ rec, const float* __restrict__ ofs,
+                                             const FanGeo<float>& gg, int64_t a, int64_t Q) {
+  const float R = gg.R;
+  const float R_sqr_inv = 1.0f / (R * R);
+  const float dxi_sqr_inv = 1.0f / (gg.delta_xi * gg.delta_xi);
+  const float* o = ofs + 8 * a;
+  const float qx = ldg(o + 2), qy = ldg(o + 3);
+  const float ddx = (ldg(o + 4) - qx) * R_sqr_inv, ddy = (ldg(o + 5) - qy) * R_sqr_inv;
+  const float dx = ldg(o) * dxi_sqr_inv, dy = ldg(o + 1) * dxi_sqr_inv;
+  const float tz = -fmaf(ddx, qx, ddy * qy), sz = -fmaf(dx, qx, dy * qy);
+  rec[0] = make_float4(ddx, ddx, ddy, ddy);
+  rec[1] = make_float4(tz, tz, dx, dx);
+  rec[2] = make_float4(dy, dy, sz, sz);
+  rec[3] = make_float4(ldg(ofs + 8 * a + 6) / R, ldg(ofs + 8 * (a + Q) + 6) / R,
+                       ldg(ofs + 8 * (a + 2 * Q) + 6) / R, ldg(ofs + 8 * (a + 3 * Q) + 6) / R);
+}
+
+// Each slice's copy: Q rows of Ns + kOrbitRowPad float4, then the Q base
+// angles' records (kOrbitRec float4 each), written by the last column of
+// blocks.
 template <int SO>
 __global__ void __launch_bounds__(256)
-orbit_rows(const float* __restrict__ sino, const float* __restrict__ sdpd, Dims d,
-           float4* __restrict__ rows4, int64_t z0, const int* __restrict__ skip) {
+orbit_rows(const float* __restrict__ sino, const float* __restrict__ sdpd,
+           const float* __restrict__ ofs, FanGeo<float> gg, Dims d, float4* __restrict__ rows4,
+           int64_t z0, const int* __restrict__ skip) {
   if (skip != nullptr && *skip) return;
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t a = blockIdx.y;
-  if (s >= d.Ns) return;
-  int64_t ss_, sa_, sz_;
-  sino_strides<SO>(d, ss_, sa_, sz_);
+  const int64_t nrow = d.Ns + kOrbitRowPad;
   const int64_t Q = d.Na / 4;
-  const float* p = sino + s * ss_ + a * sa_ + (z0 + blockIdx.z) * sz_;
-  const float w = ldg(sdpd + s);
-  rows4[((int64_t)blockIdx.z * Q + a) * d.Ns + s] =
-      make_float4(w * ldg(p), w * ldg(p + Q * sa_), w * ldg(p + 2 * Q * sa_),
-                  w * ldg(p + 3 * Q * sa_));
+  float4* copy = rows4 + (int64_t)blockIdx.z * Q * (nrow + kOrbitRec);
+  if (blockIdx.x == gridDim.x - 1) {
+    if (threadIdx.x == 0) orbit_record(copy + Q * nrow + kOrbitRec * a, ofs, gg, a, Q);
+    return;
+  }
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // padded position
+  if (e >= nrow) return;
+  const int64_t s = e - 1;
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (s >= 0 && s < d.Ns) {
+    int64_t ss_, sa_, sz_;
+    sino_strides<SO>(d, ss_, sa_, sz_);
+    const float* p = sino + s * ss_ + a * sa_ + (z0 + blockIdx.z) * sz_;
+    const float w = ldg(sdpd + s);
+    v = make_float4(w * ldg(p), w * ldg(p + Q * sa_), w * ldg(p + 2 * Q * sa_),
+                    w * ldg(p + 3 * Q * sa_));
+  }
+  copy[a * nrow + e] = v;
 }
 
 // Backprojection over quarter-turn pixel orbits.  With the maps powers of
@@ -1042,16 +1147,14 @@ orbit_rows(const float* __restrict__ sino, const float* __restrict__ sdpd, Dims 
 // each to the four sinogram rows a + j Na/4, i.e. one reciprocal, one floor
 // and two sdpd loads serve four pixel-angles.  The sinogram values are read
 // directly (the rows of the four angles are L1/L2 resident; no staging, no
-// barrier in the angle loop); with ROWS4 they come from the interleaved copy
-// made by orbit_rows, two float4 loads per pixel and base angle instead of
-// ten scalar loads.  The G thread groups of a block take interleaved base
-// angles and are added in a fixed order at the end.
-template <int IO, int SO, int G, bool ROWS4, class Epi>
+// barrier in the angle loop).  The G thread groups of a block take
+// interleaved base angles and are added in a fixed order at the end.  This
+// form runs without scratch; fan_bwd_orbit_rows below reads the row copy.
+template <int IO, int SO, int G, class Epi>
 __global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
-fan_bwd_orbit(const float* __restrict__ sino, const float4* __restrict__ rows4,
-              const float* __restrict__ ofs, const float* __restrict__ sdpd, FanGeo<float> gg,
-              Dims d, QuarterMaps qm, Epi epi, double* __restrict__ partials,
-              const int* __restrict__ skip, int64_t z0) {
+fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
+              const float* __restrict__ sdpd, FanGeo<float> gg, Dims d, QuarterMaps qm, Epi epi,
+              double* __restrict__ partials, const int* __restrict__ skip, int64_t z0) {
   constexpr int kOrbit = 4;
   constexpr int kRowsT = kBwdTileSlow / G;  // quadrant rows of the block tile
   __shared__ double red[32];
@@ -1089,7 +1192,6 @@ fan_bwd_orbit(const float* __restrict__ sino, const float4* __restrict__ rows4,
   const Off ss = (Off)ss_, sa = (Off)sa_;
   const int64_t z = z0 + blockIdx.z;
   sino += z * sz_;
-  if constexpr (ROWS4) rows4 += (int64_t)blockIdx.z * (d.Na / kOrbit) * d.Ns;
   const int Ns = (int)d.Ns;
   float acc[kOrbit];
 #pragma unroll
@@ -1131,27 +1233,12 @@ fan_bwd_orbit(const float* __restrict__ sino, const float4* __restrict__ rows4,
       const bool okm = (unsigned)xm < (unsigned)Ns;
       const bool okp = (unsigned)(xm + 1) < (unsigned)Ns;
       const int im = okm ? xm : 0, ip = okp ? xm + 1 : 0;
-      if constexpr (ROWS4) {
-        // the four rows of the orbit, premultiplied by sdpd, in one load
-        const float Wm = okm ? (1.0f - fr) * inv : 0.0f;
-        const float Wp = okp ? fr * inv : 0.0f;
-        const float4 v0 = __ldg(rows4 + (int64_t)a * Ns + im);
-        const float4 v1 = __ldg(rows4 + (int64_t)a * Ns + ip);
-        const float vm[kOrbit] = {v0.x, v0.y, v0.z, v0.w};
-        const float vp[kOrbit] = {v1.x, v1.y, v1.z, v1.w};
+      const float Wm = okm ? (1.0f - fr) * inv * ldg(sdpd + im) : 0.0f;
+      const float Wp = okp ? fr * inv * ldg(sdpd + ip) : 0.0f;
 #pragma unroll
-        for (int j = 0; j < kOrbit; ++j) {
-          const float v = fmaf(Wp, vp[j], Wm * vm[j]);
-          acc[(i + j) % kOrbit] = fmaf(wj[j], v, acc[(i + j) % kOrbit]);
-        }
-      } else {
-        const float Wm = okm ? (1.0f - fr) * inv * ldg(sdpd + im) : 0.0f;
-        const float Wp = okp ? fr * inv * ldg(sdpd + ip) : 0.0f;
-#pragma unroll
-        for (int j = 0; j < kOrbit; ++j) {
-          const float v = fmaf(Wp, ldg(row[j] + ip * ss), Wm * ldg(row[j] + im * ss));
-          acc[(i + j) % kOrbit] = fmaf(wj[j], v, acc[(i + j) % kOrbit]);
-        }
+      for (int j = 0; j < kOrbit; ++j) {
+        const float v = fmaf(Wp, ldg(row[j] + ip * ss), Wm * ldg(row[j] + im * ss));
+        acc[(i + j) % kOrbit] = fmaf(wj[j], v, acc[(i + j) % kOrbit]);
       }
     }
   }
@@ -1176,6 +1263,151 @@ fan_bwd_orbit(const float* __restrict__ sino, const float4* __restrict__ rows4,
 #pragma unroll
     for (int k = 0; k < kOrbit; ++k)
       part += epi(ox[k], oy[k], z, img_index<IO>(ox[k], oy[k], z, d), acc[k]);
+  }
+  if (Epi::kReduce) {
+    const double t = block_sum(part, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
+  }
+}
+
+// Backprojection over quarter-turn pixel orbits from the padded row copy
+// (orbit_rows): same orbit decomposition as fan_bwd_orbit, restructured to
+// issue fewer instructions per pixel-angle.
+//  * Each base angle's geometry comes from the copy's record table (four
+//    16-byte loads that every lane of a warp shares: the G thread groups
+//    take interleaved base angles, one angle per warp at a time; computed
+//    once per block into shared memory instead, the records' prologue and
+//    barriers measured slower).
+//  * Interpolation positions are clamped to [-1, Ns] (padded [0, Ns + 1]),
+//    where the copy holds zeros, instead of testing both bins.
+//  * Pairs of values go through Blackwell's packed float32 arithmetic
+//    (__ffma2_rn and friends: two lanes of one 64-bit register pair per
+//    instruction): t and s of two orbit pixels at once, and the four rows'
+//    interpolation and weighting as two pairs.  Pixel i's geometry applied to
+//    row j adds to pixel (i + j) mod 4: even i add to the pairs (0, 1) and
+//    (2, 3), odd i to the pairs (1, 2) and (3, 0), and the two pair sets are
+//    added at the end.
+// Every value is rounded as in fan_bwd_orbit: t = ddx x + (ddy y + tz),
+// s likewise, xi = s / t + midpoint, weights (1 - fr) / t and fr / t, the
+// angle weight / R by division.
+template <int IO, int G, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+fan_bwd_orbit_rows(const float4* __restrict__ rows4, FanGeo<float> gg, Dims d, QuarterMaps qm,
+                   Epi epi, double* __restrict__ partials, const int* __restrict__ skip,
+                   int64_t z0) {
+  constexpr int kOrbit = 4;
+  constexpr int kRowsT = kBwdTileSlow / G;  // quadrant rows of the block tile
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const int lane = threadIdx.x, trow = threadIdx.y;
+  const int grp = trow / kRowsT, trow_t = trow % kRowsT;
+  const int half = (int)(d.Nx / 2);
+  const int Q = (int)(d.Na / kOrbit);
+  const int nrow = (int)d.Ns + kOrbitRowPad;
+  const int px0 = (int)blockIdx.x * kBwdTileFast + lane;
+  const int py0 = (int)blockIdx.y * kRowsT + trow_t;
+  const bool own = px0 < half && py0 < half;
+  // the orbit's pixels (recomputed for the epilogue rather than kept live)
+  auto orbit = [&](int (&ox)[kOrbit], int (&oy)[kOrbit]) {
+    ox[0] = px0;
+    oy[0] = py0;
+#pragma unroll
+    for (int m = 0; m < kOrbit - 1; ++m) {
+      ox[m + 1] = qm.cx[m] + qm.axx[m] * px0 + qm.axy[m] * py0;
+      oy[m + 1] = qm.cy[m] + qm.ayx[m] * px0 + qm.ayy[m] * py0;
+    }
+  };
+  float2 pxa, pxb, pya, pyb;  // pixel centres relative to the image midpoint
+  {
+    int ox[kOrbit], oy[kOrbit];
+    orbit(ox, oy);
+    pxa = make_float2((float)ox[0] - gg.midx, (float)ox[1] - gg.midx);
+    pxb = make_float2((float)ox[2] - gg.midx, (float)ox[3] - gg.midx);
+    pya = make_float2((float)oy[0] - gg.midy, (float)oy[1] - gg.midy);
+    pyb = make_float2((float)oy[2] - gg.midy, (float)oy[3] - gg.midy);
+  }
+  // position in the padded row: detector position + 1
+  const float2 mid2 = make_float2(gg.mid_det + 1.0f, gg.mid_det + 1.0f);
+  const float hi = (float)d.Ns + 1.0f;
+  const int64_t z = z0 + blockIdx.z;
+  rows4 += (int64_t)blockIdx.z * Q * (nrow + kOrbitRec);
+  const float4* recs = rows4 + (int64_t)Q * nrow;
+  // sums of pixels (0, 1), (2, 3) [even geometry] and (1, 2), (3, 0) [odd]
+  float2 e01 = make_float2(0.f, 0.f), e23 = e01, o12 = e01, o30 = e01;
+  for (int a = grp; a < Q; a += G) {
+    const float4* rc = recs + kOrbitRec * a;
+    const float4 r0 = __ldg(rc), r1 = __ldg(rc + 1), r2 = __ldg(rc + 2), r3 = __ldg(rc + 3);
+    const float2 ddx = make_float2(r0.x, r0.y), ddy = make_float2(r0.z, r0.w);
+    const float2 tz = make_float2(r1.x, r1.y), dx = make_float2(r1.z, r1.w);
+    const float2 dy = make_float2(r2.x, r2.y), sz = make_float2(r2.z, r2.w);
+    const float2 wlo = make_float2(r3.x, r3.y), whi = make_float2(r3.z, r3.w);
+    const float4* row = rows4 + a * nrow;
+    float2 t[2], s[2];
+    t[0] = __ffma2_rn(ddx, pxa, __ffma2_rn(ddy, pya, tz));
+    t[1] = __ffma2_rn(ddx, pxb, __ffma2_rn(ddy, pyb, tz));
+    s[0] = __ffma2_rn(dx, pxa, __ffma2_rn(dy, pya, sz));
+    s[1] = __ffma2_rn(dx, pxb, __ffma2_rn(dy, pyb, sz));
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const float2 inv = make_float2(rcp_approx(t[h].x), rcp_approx(t[h].y));
+      const float2 xi = __ffma2_rn(s[h], inv, mid2);
+      const float xc[2] = {fminf(fmaxf(xi.x, 0.0f), hi), fminf(fmaxf(xi.y, 0.0f), hi)};
+      const float iv[2] = {inv.x, inv.y};
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int i = 2 * h + e;
+        const float fl = floorf(xc[e]);
+        const float fr = xc[e] - fl;
+        const int xm = (int)fl;
+        const float wm = (1.0f - fr) * iv[e], wp = fr * iv[e];
+        const float2 Wm = make_float2(wm, wm), Wp = make_float2(wp, wp);
+        const float4 vm = __ldg(row + xm);
+        const float4 vp = __ldg(row + xm + 1);
+        const float2 vlo = __ffma2_rn(Wp, make_float2(vp.x, vp.y),
+                                      __fmul2_rn(Wm, make_float2(vm.x, vm.y)));
+        const float2 vhi = __ffma2_rn(Wp, make_float2(vp.z, vp.w),
+                                      __fmul2_rn(Wm, make_float2(vm.z, vm.w)));
+        // rows (0, 1) go to pixels (i, i + 1), rows (2, 3) to (i + 2, i + 3)
+        if (i == 0) {
+          e01 = __ffma2_rn(wlo, vlo, e01);
+          e23 = __ffma2_rn(whi, vhi, e23);
+        } else if (i == 1) {
+          o12 = __ffma2_rn(wlo, vlo, o12);
+          o30 = __ffma2_rn(whi, vhi, o30);
+        } else if (i == 2) {
+          e23 = __ffma2_rn(wlo, vlo, e23);
+          e01 = __ffma2_rn(whi, vhi, e01);
+        } else {
+          o30 = __ffma2_rn(wlo, vlo, o30);
+          o12 = __ffma2_rn(whi, vhi, o12);
+        }
+      }
+    }
+  }
+  float sum[kOrbit] = {e01.x + o30.y, e01.y + o12.x, e23.x + o12.y, e23.y + o30.x};
+  // fixed-order combination of the G angle groups
+  if constexpr (G > 1) {
+    __shared__ float cred[kBwdTileSlow][kOrbit][kBwdTileFast];
+#pragma unroll
+    for (int k = 0; k < kOrbit; ++k) cred[trow][k][lane] = sum[k];
+    __syncthreads();
+    if (grp == 0) {
+#pragma unroll
+      for (int k = 0; k < kOrbit; ++k) {
+        float t = cred[trow][k][lane];
+#pragma unroll
+        for (int q = 1; q < G; ++q) t += cred[trow + q * kRowsT][k][lane];
+        sum[k] = t;
+      }
+    }
+  }
+  double part = 0.0;
+  if (own && grp == 0) {
+    int ox[kOrbit], oy[kOrbit];
+    orbit(ox, oy);
+#pragma unroll
+    for (int k = 0; k < kOrbit; ++k)
+      part += epi(ox[k], oy[k], z, img_index<IO>(ox[k], oy[k], z, d), sum[k]);
   }
   if (Epi::kReduce) {
     const double t = block_sum(part, red);

@@ -104,9 +104,11 @@ def test_host_only_entry_points(library):
         set_maps(4, maps or [(0, -1, 1, 0, c, 0), (-1, 0, 0, -1, c, c), (0, 1, -1, 0, 0, c)])
         return work(ctypes.byref(q), 1)
 
-    assert sized(512, 768, 360) == max(512 * 512 * 16, 90 * 768 * 16)
-    assert sized(512, 4000, 400) == 100 * 4000 * 16
-    assert sized(256, 384, 360) == 90 * 384 * 16  # the backprojection's only
+    # (the row copy pads every base angle's row with 1 + 2 zero entries and
+    # holds a 4-float4 geometry record per base angle)
+    assert sized(512, 768, 360) == max(512 * 512 * 16, 90 * (768 + 3 + 4) * 16)
+    assert sized(512, 4000, 400) == 100 * (4000 + 3 + 4) * 16
+    assert sized(256, 384, 360) == 90 * (384 + 3 + 4) * 16  # the backprojection's only
     assert sized(128, 192, 360) == 0
     # stacks (from 256 * 2^20 pixel-angles per slice): one slice's copy per
     # slice, up to 8 slices per launch pair; smaller slices keep the

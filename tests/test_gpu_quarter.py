@@ -147,7 +147,9 @@ def test_orbit_scratch_and_direct_gather_agree(cuda_device, name, fwd):
     Nx, Ny = ps.img_shape
     Ns, Na = ps.sinogram_shape
     fwd_need = Nx * Ny * 16
-    bwd_need = (Na // 4) * Ns * 16 if Nx % 2 == 0 else 0
+    # row copy: Ns + 3 entries (one zero before the detector, two after) and
+    # a 4-float4 geometry record per base angle
+    bwd_need = (Na // 4) * (Ns + 3 + 4) * 16 if Nx % 2 == 0 else 0
     need = int(_lib.raw("gr_work_bytes")(ctypes.byref(g), 1))
     assert need == max(fwd_need, bwd_need)
     assert g.sym == 4 and g.work and g.work_bytes == need
