@@ -561,6 +561,52 @@ def extra_large_stack(device, iterations=3, adjoint_iterations=5, order="F"):
                         "forward + backward"}
 
 
+def extra_large_stack_full(device, iterations=500, backward_iterations=50, checkpoint_every=5):
+    """The large-stack workload as configured, measured end to end: 500 TV
+    iterations on the 2048 x 2048 x 64 fan-beam stack (F order) with the
+    differentiation truncated to the last 50 iterations (states checkpointed
+    every 5), then the backward pass of sum(U); wall time of each part (CUDA
+    events) and the peak device memory of the whole run."""
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import autograd as ga
+    from gratopy_gb300.phantom import random_ellipse_volume
+
+    nz = 64
+    ps = gg.ProjectionSettings(device, gg.FANBEAM, (2048, 2048), 1440, n_detectors=2900,
+                               detector_width=2000.0, R=2000.0, RE=1000.0)
+    vol = random_ellipse_volume(device, (2048, 2048), nz, seed=SEED, order="F")
+    sino = gg.forwardprojection(vol, ps)
+    del vol
+    nrm = gg.normest(ps, 50)
+    torch.cuda.synchronize(device)
+    torch.cuda.reset_peak_memory_stats(device)
+    f = sino.detach().requires_grad_(True)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    u = ga.tv_unrolled(f, ps, 50.0, number_iterations=iterations,
+                       checkpoint_every=checkpoint_every, slice_thickness=1.0,
+                       norm_estimate=nrm, backward_iterations=backward_iterations)
+    ev[1].record()
+    u.sum().backward()
+    ev[2].record()
+    torch.cuda.synchronize(device)
+    t_fwd = ev[0].elapsed_time(ev[1]) * 1e-3
+    t_bwd = ev[1].elapsed_time(ev[2]) * 1e-3
+    peak = torch.cuda.max_memory_allocated(device)
+    finite = bool(torch.isfinite(f.grad).all())
+    del f, u, sino
+    torch.cuda.empty_cache()
+    return {"workload": "fanbeam 2048^2 x 64 slices float32 F order, 1440 angles, 2900 "
+                        "detectors, RE=1000, R=2000; TV mu=50, slice thickness 1; "
+                        f"{iterations} iterations, backward through the last "
+                        f"{backward_iterations} (checkpoint every {checkpoint_every})",
+            "tv_forward_s": t_fwd, "backward_s": t_bwd, "total_s": t_fwd + t_bwd,
+            "tv_ms_per_iteration": t_fwd / iterations * 1e3,
+            "peak_device_memory_gb": peak / 1e9, "gradient_finite": finite}
+
+
 EXTRAS = {
     "radon256": lambda device, ps, res: extra_radon256(device, res["flush"]),
     "cg50": lambda device, ps, res: extra_cg50(device, ps, res["img"]),
@@ -570,12 +616,14 @@ EXTRAS = {
     "autograd_c": lambda device, ps, res: extra_autograd(device, order="C"),
     "large_stack": lambda device, ps, res: extra_large_stack(device),
     "large_stack_c": lambda device, ps, res: extra_large_stack(device, order="C"),
+    "large_stack_full": lambda device, ps, res: extra_large_stack_full(device),
 }
 
 
-# the C-ordered large stack is left out of the default run: its x-walk strides
-# 64 x 2048 floats per pixel and runs 3x slower than the F-ordered stack
-DEFAULT_EXTRAS = [e for e in EXTRAS if e != "large_stack_c"]
+# left out of the default run: the C-ordered large stack (its x-walk strides
+# 64 x 2048 floats per pixel and runs 3x slower than the F-ordered stack) and
+# the full 500-iteration large-stack run (about four minutes)
+DEFAULT_EXTRAS = [e for e in EXTRAS if e not in ("large_stack_c", "large_stack_full")]
 
 
 def launches_per_step(ps):
@@ -693,7 +741,7 @@ def main():
                     help="skip the secondary workloads")
     ap.add_argument("--extras", default="all",
                     help="comma list of secondary workloads: " + ",".join(EXTRAS)
-                    + " (or all: every one but large_stack_c)")
+                    + " (or all: every one but large_stack_c and large_stack_full)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 

@@ -196,17 +196,25 @@ class _TVProblem:
 class _UnrolledTV(torch.autograd.Function):
     @staticmethod
     def forward(ctx, f, ps, mu, iterations, checkpoint_every, slice_thickness,
-                stepsize_weighting, norm_estimate):
+                stepsize_weighting, norm_estimate, backward_iterations):
         f = _as_contiguous(f.detach())
         prob = _TVProblem(f, ps, mu, slice_thickness, stepsize_weighting, norm_estimate)
         k = max(1, int(checkpoint_every))
+        # differentiate through the last `backward_iterations` iterations: the
+        # state entering them is kept (the first checkpoint) and treated as
+        # constant by the backward pass
+        start = iterations - min(iterations, int(backward_iterations))
         state = prob.new_state()
-        checkpoints = {0: prob.new_state()}
+        checkpoints = {}
         with torch.cuda.device(f.device):
             for i in range(iterations):
+                if i == start:
+                    checkpoints[i] = prob.new_state().copy_from(state)
                 prob.step(state)
-                if (i + 1) % k == 0 and (i + 1) < iterations:
+                if i + 1 > start and (i + 1 - start) % k == 0 and (i + 1) < iterations:
                     checkpoints[i + 1] = prob.new_state().copy_from(state)
+            if start == iterations:
+                checkpoints[start] = prob.new_state()
         ctx.prob, ctx.checkpoints, ctx.k, ctx.iterations = prob, checkpoints, k, iterations
         out = core.empty(prob.img_shape, f.dtype, prob.order, f.device)
         out.copy_(state.U)
@@ -231,19 +239,28 @@ class _UnrolledTV(torch.autograd.Function):
                     states.append(s)
                 for j in range(stop - 1, c - 1, -1):
                     prob.adjoint_step(states[j - c], states[j - c + 1], adj, tmp, gf)
-        return gf, None, None, None, None, None, None, None
+        return gf, None, None, None, None, None, None, None, None
 
 
 def tv_unrolled(sino, projectionsetting, mu, number_iterations=20, checkpoint_every=5,
-                slice_thickness=1.0, stepsize_weighting=10.0, norm_estimate=None):
+                slice_thickness=1.0, stepsize_weighting=10.0, norm_estimate=None,
+                backward_iterations=None):
     """Differentiable ``number_iterations`` steps of gratopy's TV primal-dual method.
 
     Returns the primal iterate U (as :func:`gratopy_gb300.total_variation`
     does); gradients flow to ``sino``.  ``norm_estimate`` defaults to one
     :func:`gratopy_gb300.normest` call (not differentiated).
+    ``backward_iterations`` (default: all) truncates the differentiation to
+    the last that many iterations: the state entering them is kept as the
+    first checkpoint and treated as constant, so memory and backward time
+    scale with the truncated length; states are checkpointed every
+    ``checkpoint_every`` iterations from there.
     """
     if norm_estimate is None:
         norm_estimate = core.normest(projectionsetting)
+    last = int(number_iterations) if backward_iterations is None else int(backward_iterations)
+    if last < 0:
+        raise ValueError("backward_iterations must be non-negative")
     return _UnrolledTV.apply(sino, projectionsetting, float(mu), int(number_iterations),
                              int(checkpoint_every), float(slice_thickness),
-                             float(stepsize_weighting), float(norm_estimate))
+                             float(stepsize_weighting), float(norm_estimate), last)

@@ -243,6 +243,10 @@ inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
     const int qb = (32 / (2 * split)) * (kFwdBlock / 32) * group;
     return dim3((g->Ns + qb - 1) / qb, g->Na / 4, Nz);
   }
+  if (g->dtype == GR_F32 && g->kind == GR_RADON && Nz == 1) {  // 2 * split lanes per group
+    const int rb = (32 / (2 * split)) * (kFwdBlock / 32) * group;
+    return dim3((g->Ns + rb - 1) / rb, g->Na, 1);
+  }
   return dim3((g->Ns + per_block - 1) / per_block, g->Na, (Nz + ZB - 1) / ZB);
 }
 
@@ -280,8 +284,17 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
   const dim3 grid = fwd_grid(g, Nz, SPLIT);
   if constexpr (std::is_same<T, float>::value) {
     if (g->kind == GR_RADON) {
-      fast::radon_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
-          img, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi, partials, skip);
+      if constexpr (ZB == 1) {
+        // single slices run twice the lanes per bin group (fwd_grid): one
+        // Radon slice is too small to fill the GPU with SPLIT lanes
+        fast::radon_fwd_fast<SO, IO, 1, 2 * SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+            img, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi, partials,
+            skip);
+      } else {
+        fast::radon_fwd_fast<SO, IO, ZB, SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+            img, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi, partials,
+            skip);
+      }
     } else if (use_quarter(g, Nz)) {
       // the orbit forward runs twice the lanes per bin group: its rows are
       // shared by four angles, so the wider split (and twice the blocks)

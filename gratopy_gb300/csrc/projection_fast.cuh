@@ -581,9 +581,31 @@ __device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ 
       const int x_high = min((int)((c_hi - dd) * ow), Nxx - 1);
       const float* p = img0 + (int64_t)y * step_y + (int64_t)x_low * step_x;
       float pos = fmaf((float)x_low, ox, dd);
-      // two candidates per trip for single slices (measured: 256^2 Radon
-      // forward 43.7 -> 37 us; the fan loop, with its reciprocal, loses)
-#pragma unroll(ZB == 1 ? 2 : 1)
+      if constexpr (ZB == 1) {
+        // single slices: branch-free hat weights (a zero weight adds zero)
+        // and the four bins' sums as two register pairs, updated by packed
+        // float32 multiply-adds; two candidates per trip (measured: 256^2
+        // Radon forward 43.7 -> 37 us with the unrolled loop)
+        float2 s01 = make_float2(acc[0][0], acc[1][0]), s23 = make_float2(acc[2][0], acc[3][0]);
+#pragma unroll 2
+        for (int x = x_low; x <= x_high; ++x) {
+          const float v = ldg(p);
+          const float2 v2 = make_float2(v, v);
+          const float2 w01 = make_float2(fmaxf(0.0f, 1.0f - fabsf(pos)),
+                                         fmaxf(0.0f, 1.0f - fabsf(pos - 1.0f)));
+          const float2 w23 = make_float2(fmaxf(0.0f, 1.0f - fabsf(pos - 2.0f)),
+                                         fmaxf(0.0f, 1.0f - fabsf(pos - 3.0f)));
+          s01 = __ffma2_rn(w01, v2, s01);
+          s23 = __ffma2_rn(w23, v2, s23);
+          pos += ox;
+          p += step_x;
+        }
+        acc[0][0] = s01.x;
+        acc[1][0] = s01.y;
+        acc[2][0] = s23.x;
+        acc[3][0] = s23.y;
+        continue;
+      }
       for (int x = x_low; x <= x_high; ++x) {
         float v[ZB];
         load_slices<IO, ZB>(v, p, sz, zn, d.vec4, 1.0f);

@@ -162,9 +162,11 @@ def test_unrolled_tv_matches_finite_differences(cuda_device, geom, nz, slice_thi
     assert rel_l2(f32.grad.double().cpu().numpy(), grad.cpu().numpy()) < 1e-4
 
 
-def _tv_torch(f, ps, mu, iterations, slice_thickness, norm_estimate, stepsize_weighting=10.0):
+def _tv_torch(f, ps, mu, iterations, slice_thickness, norm_estimate, stepsize_weighting=10.0,
+              detach_at=None):
     """gratopy's TV primal-dual iteration (total_variation.cl:54-167,
-    gratopy.py:2686-2717) in torch operations, differentiated by torch."""
+    gratopy.py:2686-2717) in torch operations, differentiated by torch; the
+    state entering iteration ``detach_at`` is cut from the graph."""
     import torch
     import torch.nn.functional as Fn
 
@@ -187,7 +189,9 @@ def _tv_torch(f, ps, mu, iterations, slice_thickness, norm_estimate, stepsize_we
     U = torch.zeros(p.img_shape, dtype=f.dtype, device=f.device)
     Ubar, L = U, torch.zeros_like(f)
     V = [U, U, U]
-    for _ in range(iterations):
+    for i in range(iterations):
+        if i == detach_at:
+            U, Ubar, L, V = U.detach(), Ubar.detach(), L.detach(), [v.detach() for v in V]
         g = [forward_diff(Ubar, 0), forward_diff(Ubar, 1),
              forward_diff(Ubar, 2) / p.z if three else torch.zeros_like(Ubar)]
         W = [V[i] + p.sigma * g[i] for i in range(3)]
@@ -227,6 +231,36 @@ def test_unrolled_tv_adjoint_equals_autograd_of_restatement(cuda_device, geom, n
     (ub * c).sum().backward()
     assert rel_l2(ua.detach().cpu().numpy(), ub.detach().cpu().numpy()) < 1e-12
     assert rel_l2(fa.grad.cpu().numpy(), fb.grad.cpu().numpy()) < 1e-12
+
+
+@pytest.mark.parametrize("geom", ["radon", "fan"])
+def test_unrolled_tv_truncated_backward(cuda_device, geom):
+    """Differentiation through the last 7 of 17 iterations (checkpoints every
+    3 from iteration 10) equals torch autograd of the restatement with its
+    state cut from the graph at iteration 10; the forward value is the full
+    17-iteration one."""
+    import torch
+
+    from gratopy_gb300 import autograd as ga
+    import gratopy_gb300 as gg
+
+    ps = device_settings(CFG[geom], cuda_device)
+    x = _rand(ps.img_shape, torch.float64, cuda_device, 21) + 0.5
+    f = (gg.forwardprojection(x, ps) + 0.01 * _rand(ps.sinogram_shape, torch.float64,
+                                                      cuda_device, 22)).detach()
+    nrm = gg.normest(ps, 30, dtype="float64", x0=np.ones(ps.img_shape))
+    c = _rand(ps.img_shape, torch.float64, cuda_device, 23)
+    fa = f.clone().requires_grad_(True)
+    ua = ga.tv_unrolled(fa, ps, 20.0, number_iterations=17, checkpoint_every=3,
+                        slice_thickness=0.0, norm_estimate=nrm, backward_iterations=7)
+    (ua * c).sum().backward()
+    fb = f.clone().requires_grad_(True)
+    ub = _tv_torch(fb, ps, 20.0, 17, 0.0, nrm, detach_at=10)
+    (ub * c).sum().backward()
+    assert rel_l2(ua.detach().cpu().numpy(), ub.detach().cpu().numpy()) < 1e-12
+    assert rel_l2(fa.grad.cpu().numpy(), fb.grad.cpu().numpy()) < 1e-12
+    full = ga.tv_unrolled(f, ps, 20.0, number_iterations=17, norm_estimate=nrm)
+    assert torch.equal(ua.detach(), full)
 
 
 def test_tv_unrolled_forward_equals_total_variation(cuda_device):

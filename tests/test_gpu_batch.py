@@ -69,10 +69,14 @@ def test_batched_matches_per_call(cuda_device):
     for pr, got in zip(problems, results):
         ps = pr.settings
         # the per-call form with the batched launch shapes (one thread row per
-        # angle set in the backprojection, every angle's own forward), so both
-        # add in the same order
-        ps.gr_geometry(np.float32).bwd_split = 1
-        ps.gr_geometry(np.float32).sym = 0
+        # angle set in the backprojection, every angle's own forward, and for
+        # Radon the batch's lanes per bin group: a per-call single Radon
+        # slice runs twice fwd_split lanes), so both add in the same order
+        g = ps.gr_geometry(np.float32)
+        g.bwd_split = 1
+        g.sym = 0
+        if ps.is_parallel:
+            g.fwd_split = pr.fwd_split // 2
         if pr.solver in ("landweber", "tv"):
             want_n = gg.normest(ps, 20, x0=pr.normest_x0)
             assert abs(pr.norm_estimate - want_n) <= 1e-12 * want_n
