@@ -110,120 +110,13 @@ __device__ __forceinline__ void stage_windows(Window<ZB>& win, const Rec* rec, i
   }
 }
 
-// ----------------------------------------------------- bulk-copy staging
-// One block-wide mbarrier tracks the bulk copies (cp.async.bulk, the TMA
-// unit's untiled global -> shared copy) that stage detector windows.  Every
-// wait is bounded: after kStageSpin unsuccessful polls the block waits once
-// more (again bounded) for its own copies and reports the failure through
-// its outputs (NaN), so a fault of the copy engine cannot hang the kernel.
-constexpr int kStageSpin = 1 << 22;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
-               : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
-  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile(
-      "{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
-  for (int it = 0; it < kStageSpin; ++it) {
-    unsigned done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-// bytes (a multiple of 16) from 16-byte aligned global src to 16-byte
-// aligned shared dst, completing on bar
-__device__ __forceinline__ void bulk_copy_to_smem(void* dst, const void* src, unsigned bytes,
-                                                  uint64_t* bar) {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Stage the windows of angles [a0, a0 + na) of an F-ordered single-slice
-// sinogram: the part of each window that lies on the detector and starts and
-// ends on 16-byte boundaries of the sinogram arrives by one bulk copy per
-// angle (issued by lane 0 of the angle's warp); the ragged ends and the bins
-// off the detector (zeros) are written by the warp's lanes.  A record's ws
-// is aligned (sinogram element (a0 + j) Ns + ws on a 16-byte boundary) by
-// construction.  Every thread of the block arrives on bar once; returns
-// false when the copies did not complete within the polling limit.
-template <class Rec>
-__device__ __forceinline__ bool stage_windows_bulk(Window<1>& win, const Rec* rec, int na, int a0,
-                                                   const float* __restrict__ sino, int Ns,
-                                                   uint64_t* bar, unsigned& phase) {
-  const int lane = threadIdx.x, warp = threadIdx.y;
-  for (int j = warp; j < na; j += (int)blockDim.y) {
-    const int ws = rec[j].ws, wn = rec[j].wn;
-    if (ws == INT_MIN) continue;
-    const float* row = sino + (int64_t)(a0 + j) * Ns;
-    const int c0 = ws >= 0 ? ws : ws + ((-ws + 3) & ~3);  // first aligned bin >= 0
-    const int end = min(ws + wn, Ns);
-    const int c1 = end > c0 ? c0 + ((end - c0) & ~3) : c0;  // aligned end <= end
-    if (lane == 0 && c1 > c0) {
-      mbar_expect_tx(bar, (unsigned)(c1 - c0) * 4u);
-      bulk_copy_to_smem(&win.v[j][0][c0 - ws], row + c0, (unsigned)(c1 - c0) * 4u, bar);
-    }
-    const int left = min(c0 - ws, wn);
-    for (int k = lane; k < left; k += 32) {
-      const int b = ws + k;
-      win.v[j][0][k] = (b >= 0 && b < Ns) ? ldg(row + b) : 0.0f;
-    }
-    for (int k = c1 - ws + lane; k < wn; k += 32) {
-      const int b = ws + k;
-      win.v[j][0][k] = (b >= 0 && b < Ns) ? ldg(row + b) : 0.0f;
-    }
-  }
-  mbar_arrive(bar);
-  bool ok = mbar_wait_bounded(bar, phase);
-  if (!ok) mbar_wait_bounded(bar, phase);  // the block's own copies, once more
-  phase ^= 1u;
-  return ok;
-}
-
 template <int IO, int SO, int ZB, int ASPLIT, int PY, class Epi>
 __device__ __forceinline__ double radon_bwd_fast_tile(const float* __restrict__ sino, const float* __restrict__ ofs, Dims d, Epi epi,
                uint3 bid) {
   using TL = Tile<ASPLIT, PY>;
   constexpr int kWinAngles = WinAngles<ZB>::value;
   __shared__ RadonRec rec[kWinAngles];
-  __shared__ __align__(16) Window<ZB> win;
-  // F-ordered single slices on a 16-byte aligned sinogram stage their windows
-  // by bulk copies (see stage_windows_bulk)
-  constexpr bool kBulk = SO == ORDER_F && ZB == 1;
-  __shared__ uint64_t bar;
-  const bool bulk = kBulk && (reinterpret_cast<uintptr_t>(sino) & 15u) == 0;
-  unsigned phase = 0;
-  bool staged_ok = true;
+  __shared__ Window<ZB> win;
   const int g = threadIdx.y % ASPLIT;
   const int64_t f0 = (int64_t)bid.x * kBwdTileFast;
   const int64_t s0 = (int64_t)bid.y * TL::kSlow;
@@ -245,10 +138,6 @@ __device__ __forceinline__ double radon_bwd_fast_tile(const float* __restrict__ 
 #pragma unroll
     for (int k = 0; k < ZB; ++k) acc[p][k] = 0.0f;
   const int tid = threadIdx.x + kBwdTileFast * threadIdx.y;
-  if (bulk) {
-    if (tid == 0) mbar_init(&bar, blockDim.x * blockDim.y);
-    __syncthreads();
-  }
   float cxs[PY], cys[PY];
 #pragma unroll
   for (int p = 0; p < PY; ++p) {
@@ -265,15 +154,8 @@ __device__ __forceinline__ double radon_bwd_fast_tile(const float* __restrict__ 
       const float lo = off + fminf(fx0 * X, fx1 * X) + fminf(fy0 * Y, fy1 * Y);
       const float hi = off + fmaxf(fx0 * X, fx1 * X) + fmaxf(fy0 * Y, fy1 * Y);
       const bool finite = lo > -1e9f && hi < 1e9f;
-      int w0 = finite ? (int)floorf(lo) - 1 : 0;
-      int wn = finite ? (int)floorf(hi) + 3 - w0 : kWin + 1;
-      if (bulk && finite) {
-        // start the window on a 16-byte boundary of the sinogram row
-        const int64_t e = (int64_t)(a0 + tid) * Ns + w0;
-        const int back = (int)(((e % 4) + 4) % 4);
-        w0 -= back;
-        wn += back;
-      }
+      const int w0 = finite ? (int)floorf(lo) - 1 : 0;
+      const int wn = finite ? (int)floorf(hi) + 3 - w0 : kWin + 1;
       const bool fits = finite && wn <= kWin;
       RadonRec r;
       r.r = make_float4(X, Y, fits ? off - (float)w0 : off, o[4]);
@@ -282,14 +164,7 @@ __device__ __forceinline__ double radon_bwd_fast_tile(const float* __restrict__ 
       rec[tid] = r;
     }
     const int all_fit = __syncthreads_and(tid >= na || rec[tid].ws != INT_MIN);
-    if constexpr (kBulk) {
-      if (bulk)
-        staged_ok &= stage_windows_bulk(win, rec, na, a0, sino, Ns, &bar, phase);
-      else
-        stage_windows<SO, ZB, false>(win, rec, na, a0, sino, nullptr, d, z0, zn);
-    } else {
-      stage_windows<SO, ZB, false>(win, rec, na, a0, sino, nullptr, d, z0, zn);
-    }
+    stage_windows<SO, ZB, false>(win, rec, na, a0, sino, nullptr, d, z0, zn);
     __syncthreads();
     if (all_fit && na == kWinAngles) {
       // common case: every window staged, no per-angle branch
@@ -338,16 +213,6 @@ __device__ __forceinline__ double radon_bwd_fast_tile(const float* __restrict__ 
         }
       }
     }
-    }
-  }
-  if (bulk) {
-    __syncthreads();  // no thread still polls the barrier
-    if (tid == 0) mbar_inval(&bar);
-    if (!staged_ok) {  // report a copy that did not complete
-#pragma unroll
-      for (int p = 0; p < PY; ++p)
-#pragma unroll
-        for (int k = 0; k < ZB; ++k) acc[p][k] = __int_as_float(0x7fc00000);
     }
   }
   // fixed-order combination of the ASPLIT angle groups
@@ -739,7 +604,8 @@ __device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ 
         acc[1][0] = s01.y;
         acc[2][0] = s23.x;
         acc[3][0] = s23.y;
-      } else {
+        continue;
+      }
       for (int x = x_low; x <= x_high; ++x) {
         float v[ZB];
         load_slices<IO, ZB>(v, p, sz, zn, d.vec4, 1.0f);
@@ -753,7 +619,6 @@ __device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ 
         }
         pos += ox;
         p += step_x;
-      }
       }
     }
   }
