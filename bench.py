@@ -783,7 +783,10 @@ def main():
     # backprojection's orbits need an even side)
     quarter = ps.gr_geometry(np.float32).sym == 4
     fwd_name = "fan_fwd_quarter" if quarter else "fan_fwd_fast"
-    bwd_name = "fan_bwd_orbit" if quarter and Nx % 2 == 0 else "fan_bwd_fast"
+    if quarter and Nx % 2 == 0:  # with scratch bound, from the interleaved row copy
+        bwd_name = "fan_bwd_orbit_rows" if ps.gr_geometry(np.float32).work else "fan_bwd_orbit"
+    else:
+        bwd_name = "fan_bwd_fast"
     dom, t_dom = (fwd_name, fwd) if fwd >= bwd else (bwd_name, bwd)
     # DRAM traffic and issue utilisation of the dominant kernel from the
     # committed ncu summary of this workload (one capture, not this run)
