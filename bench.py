@@ -448,13 +448,24 @@ def extra_batched(device, small=False, fp64_every=4):
         e = float(torch.linalg.norm(out_b[k].double() - b) / torch.linalg.norm(b))
         err64[p.solver] = max(err64.get(p.solver, 0.0), e)
     t64 = time.perf_counter() - t64
+    # pixel-angles the solves project: normest (50 iterations of A then A^T
+    # for Landweber and TV), the CG start (A x0, A^T d), two per iteration
+    pa = 0
+    for p in probs:
+        Nx, Ny = p.settings.img_shape
+        per = Nx * Ny * p.settings.n_angles
+        n = 2 * p.iterations + (2 if p.solver == "cg" else 2 * 50)
+        pa += n * per
     name = ("64 problems, side U{32..128}, angles U[30,180]" if small else
             "64 problems, side U{128,192,256,384,512}, angles U[60,720]")
     return {"workload": name + ", half Radon (full or 2pi/3 range) half fan beam, "
                         "Landweber-200 / CG-50 / TV-100, float32, normest included",
             "batched_recon_per_s": 64 / t_b, "plain_graph_recon_per_s": 64 / t_pg,
             "plain_direct_recon_per_s": 64 / t_pd, "speedup_vs_plain_direct": t_pd / t_b,
-            "speedup_vs_plain_graph": t_pg / t_b, "max_rel_err_vs_per_call": err,
+            "speedup_vs_plain_graph": t_pg / t_b,
+            "batched_gpixel_angle_per_s": pa / t_b / 1e9,
+            "plain_direct_gpixel_angle_per_s": pa / t_pd / 1e9,
+            "pixel_angles_projected": pa, "max_rel_err_vs_per_call": err,
             "max_rel_err_vs_fp64": err64,
             "fp64_reference": f"float64 per-call solves of every {fp64_every}th problem "
                               f"({len(range(0, len(solved), fp64_every))} of {len(solved)}) "

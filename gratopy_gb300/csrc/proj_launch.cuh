@@ -240,8 +240,9 @@ inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   const int group = g->dtype == GR_F32 ? fast::kRayGroup : 1;  // bins per lane group
   const int per_block = (32 / split) * (kFwdBlock / 32) * group;
   if (use_quarter(g, Nz)) {  // one slice per block, 2 * split lanes per group
-    const int qb = (32 / (2 * split)) * (kFwdBlock / 32) * group;
-    return dim3((g->Ns + qb - 1) / qb, g->Na / 4, Nz);
+    const int apb = fast::kQuarterAnglesPerBlock;
+    const int qb = (32 / (2 * split)) * (kFwdBlock / 32 / apb) * group;
+    return dim3((g->Ns + qb - 1) / qb, (g->Na / 4 + apb - 1) / apb, Nz);
   }
   if (g->dtype == GR_F32 && g->kind == GR_RADON && Nz == 1) {  // 2 * split lanes per group
     const int rb = (32 / (2 * split)) * (kFwdBlock / 32) * group;

@@ -801,6 +801,29 @@ fan_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs,
 // the projection of the turned image at angle a.  Index maps: pixel (x, y)
 // of the base angle is pixel (cx + axx x + axy y, cy + ayx x + ayy y) for
 // angle a + m Na/4.
+// Lane layout of the orbit forward: a block's warps are split over
+// kAnglesPerBlock adjacent base angles, each angle's warps covering the same
+// bins, so the image strips the block streams overlap in L1 (adjacent base
+// angles differ by 360/Na degrees).  Within a warp, 32 / SPLIT groups of
+// SPLIT lanes each own kRayGroup adjacent bins.
+constexpr int kQuarterAnglesPerBlock = 2;
+
+template <int SPLIT>
+struct QuarterLayout {
+  static constexpr int kGroupsPerWarp = 32 / SPLIT;
+  static constexpr int kWarpsPerAngle = (kFwdBlock / 32) / kQuarterAnglesPerBlock;
+  static constexpr int kBinsPerBlock = kGroupsPerWarp * kRayGroup * kWarpsPerAngle;
+  int64_t s0, a;
+  int lane_group;
+  __device__ __forceinline__ explicit QuarterLayout(uint3 bid) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    a = (int64_t)bid.y * kQuarterAnglesPerBlock + warp / kWarpsPerAngle;
+    s0 = (int64_t)bid.x * kBinsPerBlock +
+         ((int64_t)(warp % kWarpsPerAngle) * kGroupsPerWarp + lane % kGroupsPerWarp) * kRayGroup;
+    lane_group = lane / kGroupsPerWarp;
+  }
+};
+
 struct QuarterMaps {
   int axx[3], axy[3], ayx[3], ayy[3], cx[3], cy[3];
   // nonzero when map m is the m-th power of one quarter turn: then the
@@ -820,11 +843,11 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
                                                        Epi epi, uint3 bid, int64_t z) {
   constexpr int kOrbit = 4;
   using Off = typename std::conditional<IO == ORDER_C && !PIX4, int64_t, int>::type;
-  const GroupLayout<SPLIT> L(bid);
+  const QuarterLayout<SPLIT> L(bid);
   const int64_t s0 = L.s0;
-  const int64_t a = bid.y;              // base angle in [0, Na/4)
+  const int64_t a = L.a;                // base angle in [0, Na/4)
   const int64_t quarter = d.Na / kOrbit;
-  const bool active = s0 < d.Ns;
+  const bool active = s0 < d.Ns && a < quarter;
   // bin q's sums for the orbit angles (0, 1) and (2, 3): one register pair
   // each, updated by packed float32 multiply-adds (two lanes per instruction)
   float2 acc01[kRayGroup], acc23[kRayGroup];
