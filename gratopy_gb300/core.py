@@ -333,7 +333,7 @@ class ProjectionSettings:
             g.geo[i] = float(v)
         maps = self.quarter_maps()
         if maps is not None:
-            g.sym = 4
+            g.sym = 4 if self.is_fan else 2
             for m, row in enumerate(maps):
                 for k, v in enumerate(row):
                     g.sym_map[m][k] = int(v)
@@ -344,12 +344,16 @@ class ProjectionSettings:
         self._work_bytes[dtype] = int(_lib.raw("gr_work_bytes")(ctypes.byref(g), 1))
 
     def quarter_maps(self):
-        """Index maps of a quarter-turn symmetric fan-beam geometry (see
-        :mod:`gratopy_gb300.symmetry`), or None; computed once."""
+        """Index maps of the geometry's orbit symmetry (see
+        :mod:`gratopy_gb300.symmetry`): the quarter-turn orbits of a fan-beam
+        geometry, the half-circle orbits (quarter turn and detector mirror)
+        of a parallel-beam one; None when the geometry has none.  Computed
+        once."""
         if not hasattr(self, "_quarter"):
-            from .symmetry import fan_quarter_maps
+            from .symmetry import fan_quarter_maps, radon_half_maps
 
-            self._quarter = fan_quarter_maps(self.struct, self.img_shape) if self.is_fan else None
+            find = fan_quarter_maps if self.is_fan else radon_half_maps
+            self._quarter = find(self.struct, self.img_shape)
         return self._quarter
 
     def forward_scale(self, dtype) -> float:

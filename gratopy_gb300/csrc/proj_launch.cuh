@@ -31,7 +31,10 @@ inline int check_geometry(const gr_geometry* g) {
   if (g->kind == GR_FANBEAM && g->sdpd == nullptr) return GR_ERR_ARG;
   if (g->Nx <= 0 || g->Ny <= 0 || g->Ns <= 0 || g->Na <= 0) return GR_ERR_SHAPE;
   if (g->sym != 0) {
-    if (g->sym != 4 || g->Nx != g->Ny) return GR_ERR_ARG;
+    // 4: fan-beam quarter-turn orbits; 2: parallel-beam half-circle orbits
+    const bool kind_ok = (g->sym == 4 && g->kind == GR_FANBEAM) ||
+                         (g->sym == 2 && g->kind == GR_RADON && g->Na % 2 == 0);
+    if (!kind_ok || g->Nx != g->Ny) return GR_ERR_ARG;
     for (int m = 0; m < 3; ++m)
       if (!valid_quarter_map(g->sym_map[m], g->Nx)) return GR_ERR_ARG;
   }
@@ -117,12 +120,13 @@ inline int fwd_split(const gr_geometry* g, int Nz) {
 }
 
 inline bool use_quarter_bwd(const gr_geometry* g, int Nz);
+inline bool use_radon_orbit_bwd(const gr_geometry* g, int Nz);
 
 inline int bwd_split(const gr_geometry* g, int Nz) {
   if (valid_split(g->bwd_split)) return clamp_split(g, g->bwd_split);
   // orbit backprojection: 8 angle groups measured fastest or within 1% of it
   // from 128^2 to 2048^2 (360 to 1440 angles)
-  if (use_quarter_bwd(g, Nz)) return 8;
+  if (use_quarter_bwd(g, Nz) || use_radon_orbit_bwd(g, Nz)) return 8;
   if (g->dtype == GR_F32) {
     // float32 tiles stage detector windows per block, so angles are split
     // over thread rows only when the image alone cannot fill 40% of the
@@ -219,7 +223,31 @@ inline size_t quarter_bwd_bytes(const gr_geometry* g, int Nz) {
          sizeof(float4);
 }
 
+// Parallel beam, float32 single slices with the half-circle orbit maps
+// (sym = 2): the orbit kernels read copies of the image (the forward, any
+// side) and of the sinogram (the backprojection, even sides), so each runs
+// only when the caller's scratch holds its copy; otherwise the per-angle
+// kernels run.
+inline bool use_radon_orbit(const gr_geometry* g, int Nz) {
+  return g->sym == 2 && g->dtype == GR_F32 && g->kind == GR_RADON && Nz == 1 &&
+         g->Na % 2 == 0 && g->Nx == g->Ny && (int64_t)g->Nx * g->Ny <= INT32_MAX &&
+         (int64_t)(g->Ns + fast::kOrbitRowPad) * (g->Na / 2) <= INT32_MAX;
+}
+
+inline size_t radon_orbit_fwd_bytes(const gr_geometry* g, int Nz) {
+  return use_radon_orbit(g, Nz) ? (size_t)g->Nx * (size_t)g->Ny * sizeof(float4) : 0;
+}
+
+inline size_t radon_orbit_bwd_bytes(const gr_geometry* g, int Nz) {
+  if (!use_radon_orbit(g, Nz) || g->Nx % 2 != 0) return 0;
+  return (size_t)(g->Na / 2) * (size_t)(g->Ns + fast::kOrbitRowPad) * sizeof(float4);
+}
+
 inline size_t orbit_work_bytes(const gr_geometry* g, int Nz) {
+  if (g->kind == GR_RADON) {
+    const size_t f = radon_orbit_fwd_bytes(g, Nz), b = radon_orbit_bwd_bytes(g, Nz);
+    return f > b ? f : b;
+  }
   const size_t f = quarter_fwd_bytes(g, Nz), b = quarter_bwd_bytes(g, Nz);
   const int slices = Nz < kQuarterCopySlices ? Nz : kQuarterCopySlices;
   return (f > b ? f : b) * (size_t)(slices > 0 ? slices : 0);
@@ -235,6 +263,15 @@ inline int work_slices(const gr_geometry* g, size_t per_slice, int Nz) {
 }
 
 
+inline bool use_radon_orbit_fwd(const gr_geometry* g, int Nz) {
+  return use_radon_orbit(g, Nz) && work_slices(g, radon_orbit_fwd_bytes(g, Nz), Nz) > 0;
+}
+
+inline bool use_radon_orbit_bwd(const gr_geometry* g, int Nz) {
+  return g->Nx % 2 == 0 && use_radon_orbit(g, Nz) &&
+         work_slices(g, radon_orbit_bwd_bytes(g, Nz), Nz) > 0;
+}
+
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   const int ZB = zblock(Nz);
   const int group = g->dtype == GR_F32 ? fast::kRayGroup : 1;  // bins per lane group
@@ -243,6 +280,12 @@ inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
     const int apb = fast::kQuarterAnglesPerBlock;
     const int qb = (32 / (2 * split)) * (kFwdBlock / 32 / apb) * group;
     return dim3((g->Ns + qb - 1) / qb, (g->Na / 4 + apb - 1) / apb, Nz);
+  }
+  if (use_radon_orbit_fwd(g, Nz)) {  // bins s < ceil(Ns/2), base angles k < Na/2
+    const int apb = fast::kQuarterAnglesPerBlock;
+    const int qb = (32 / (4 * split)) * (kFwdBlock / 32 / apb) * group;  // 4 * split lanes
+    const int H = (int)((g->Ns + 1) / 2);
+    return dim3((H + qb - 1) / qb, (g->Na / 2 + apb - 1) / apb, 1);
   }
   if (g->dtype == GR_F32 && g->kind == GR_RADON && Nz == 1) {  // 2 * split lanes per group
     const int rb = (32 / (2 * split)) * (kFwdBlock / 32) * group;
@@ -266,7 +309,7 @@ inline fast::QuarterMaps quarter_maps(const gr_geometry* g) {
 }
 
 inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
-  if (use_quarter_bwd(g, Nz)) {  // 32 x (8 / split) tiles of the quadrant x, y < N/2
+  if (use_quarter_bwd(g, Nz) || use_radon_orbit_bwd(g, Nz)) {  // 32 x (8 / split) quadrant tiles
     const int half = g->Nx / 2, rows = kBwdTileSlow / split;
     return dim3((half + kBwdTileFast - 1) / kBwdTileFast, (half + rows - 1) / rows, Nz);
   }
@@ -286,6 +329,28 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
   if constexpr (std::is_same<T, float>::value) {
     if (g->kind == GR_RADON) {
       if constexpr (ZB == 1) {
+        if (use_radon_orbit_fwd(g, Nz)) {
+          // half-circle orbits: each pixel's four orbit pixels as one float4,
+          // then the forward over the orbits
+          const fast::QuarterMaps qm = quarter_maps(g);
+          float4* img4 = static_cast<float4*>(g->work);
+          if constexpr (IO == ORDER_F) {
+            constexpr int kTile = fast::kOrbitTile;
+            const dim3 tgrid((g->Nx + kTile - 1) / kTile, (g->Ny + kTile - 1) / kTile, 1);
+            fast::orbit_pixels_tiled<IO><<<tgrid, dim3(kTile, kTile), 0, st>>>(img, d, qm, img4,
+                                                                               0, skip);
+          } else {
+            const dim3 pgrid((g->Nx + 255) / 256, g->Ny, 1);
+            fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, 0, skip);
+          }
+          // four times the lanes per group: a group's work is shared by four
+          // outputs, so the orbit forward has a quarter of the groups (256^2 x
+          // 180: 16 lanes 41.6 us, 8 lanes 63.4 us)
+          fast::radon_fwd_quarter<SO, 4 * SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
+              img4, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi,
+              partials, skip);
+          return check_launch();
+        }
         // single slices run twice the lanes per bin group (fwd_grid): one
         // Radon slice is too small to fill the GPU with SPLIT lanes
         fast::radon_fwd_fast<SO, IO, 1, 2 * SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
@@ -422,6 +487,14 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
         fast::fan_bwd_orbit<IO, SO, SPLIT, Epi><<<grid, block, 0, st>>>(
             sino, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials, skip, 0);
       }
+    } else if (use_radon_orbit_bwd(g, Nz)) {
+      // half-circle orbits: the mirror-interleaved row copy, then the
+      // backprojection over the orbits
+      float4* rows4 = static_cast<float4*>(g->work);
+      const dim3 rgrid((g->Ns + fast::kOrbitRowPad + 255) / 256, g->Na / 2, 1);
+      fast::radon_orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, d, rows4, skip);
+      fast::radon_bwd_orbit_rows<IO, SPLIT, Epi><<<grid, block, 0, st>>>(
+          rows4, static_cast<const float*>(g->ofs), d, quarter_maps(g), epi, partials, skip);
     } else if (g->kind == GR_RADON) {
       fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, fblock, 0, st>>>(
           sino, static_cast<const float*>(g->ofs), d, epi, partials, skip);

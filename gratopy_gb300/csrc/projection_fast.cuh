@@ -604,8 +604,7 @@ __device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ 
         acc[1][0] = s01.y;
         acc[2][0] = s23.x;
         acc[3][0] = s23.y;
-        continue;
-      }
+      } else {
       for (int x = x_low; x <= x_high; ++x) {
         float v[ZB];
         load_slices<IO, ZB>(v, p, sz, zn, d.vec4, 1.0f);
@@ -619,6 +618,7 @@ __device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ 
         }
         pos += ox;
         p += step_x;
+      }
       }
     }
   }
@@ -1453,6 +1453,273 @@ fan_bwd_orbit_rows(const float4* __restrict__ rows4, FanGeo<float> gg, Dims d, Q
 #pragma unroll
     for (int k = 0; k < kOrbit; ++k)
       part += epi(ox[k], oy[k], z, img_index<IO>(ox[k], oy[k], z, d), sum[k]);
+  }
+  if (Epi::kReduce) {
+    const double t = block_sum(part, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
+  }
+}
+
+// ------------------------------------------ parallel beam: half-circle orbits
+// For Na angles equispaced over [0, pi) (Na even), a square image centred on
+// the rotation axis and a detector centred on the central ray, angle
+// k + Na/2 sees the grid as angle k sees it after a quarter turn S, and
+// angle k sees the grid turned by a half with its detector reversed
+// (p(-s, phi) = p(s, phi + pi)).  With Q = Na/2 and s' = Ns - 1 - s the four
+// outputs of the cycle
+//   c = 0: (s, k)   c = 1: (s, k + Q)   c = 2: (s', k)   c = 3: (s', k + Q)
+// are the weights of angle k applied to img(P), img(S^-1 P), img(-P) and
+// img(-S^-1 P): the orbit copy of orbit_pixels with the maps
+// (S^-1, -I, -S^-1).  Detected on the host (gratopy_gb300/symmetry.py).
+
+__device__ __forceinline__ int radon_orbit_half(int64_t Ns) { return (int)((Ns + 1) / 2); }
+
+// Forward over the orbits: a lane group owns kRayGroup adjacent bins s < H =
+// ceil(Ns/2) of base angle k < Q and writes the 16 outputs of their cycles
+// (the mirrored bins s' only where s' >= H, so the middle bin of an odd
+// detector is written once).  A group walks the cycle member (k or k + Q,
+// rays turned by a quarter) whose detector coordinate changes faster along
+// the image's y axis: its lanes then take adjacent image columns and walk
+// down them, so a load instruction reads adjacent pixels of the orbit copy.
+// Two candidates per trip, packed pair sums, branch-free hat weights, as in
+// fan_fwd_quarter.
+template <int SO, int SPLIT, class Epi>
+__device__ __forceinline__ double radon_fwd_quarter_tile(const float4* __restrict__ img4,
+                                                         const float* __restrict__ ofs,
+                                                         RadonGeo<float> g, Dims d, Epi epi,
+                                                         uint3 bid) {
+  constexpr int kOrbit = 4;
+  const QuarterLayout<SPLIT> L(bid);
+  const int64_t s0 = L.s0;
+  const int64_t k = L.a;
+  const int64_t Q = d.Na / 2;
+  const int H = radon_orbit_half(d.Ns);
+  const bool active = s0 < H && k < Q;
+  float2 acc01[kRayGroup], acc23[kRayGroup];
+#pragma unroll
+  for (int q = 0; q < kRayGroup; ++q) acc01[q] = acc23[q] = make_float2(0.0f, 0.0f);
+  int shift = 0;
+  if (active) {
+    int64_t ab = k;
+    if (fabsf(ofs[8 * k + 1]) < fabsf(ofs[8 * k])) {  // walk the member turned by a quarter
+      ab = k + Q;
+      shift = 1;
+    }
+    const float X = ofs[8 * ab], Y = ofs[8 * ab + 1];
+    const float base = ofs[8 * ab + 2] - (float)(int)s0;  // xi - s0 = X x + Y y + base
+    const int N = (int)d.Nx;
+    const float yinv = 1.0f / Y;
+    // candidate y of column x: pos = xi - s0 in (-1, kRayGroup), i.e. y between
+    // lo(x) = alo + bx x and hi(x) = ahi + bx x
+    const float c_lo = yinv > 0.0f ? -1.0f : (float)kRayGroup;
+    const float c_hi = yinv > 0.0f ? (float)kRayGroup : -1.0f;
+    const float bx = -X * yinv;
+    const float alo = (c_lo - base) * yinv, ahi = (c_hi - base) * yinv;
+    int x0, x1;
+    row_range(alo, bx, ahi, bx, (float)(N - 1), N, x0, x1);
+    const int stp = N;  // the orbit copy is x-fastest
+    for (int x = x0 + L.lane_group; x <= x1; x += SPLIT) {
+      const float xf = (float)x;
+      const int ylo = max(0, (int)ceilf(fmaf(bx, xf, alo)));
+      const int yhi = min(N - 1, (int)floorf(fmaf(bx, xf, ahi)));
+      float pos = fmaf(Y, (float)ylo, fmaf(X, xf, base));
+      int o0 = ylo * stp + x;
+      for (int y = ylo; y <= yhi; y += 2) {
+        const bool two = y < yhi;
+        const float pb = pos + Y;
+        const float4 pa4 = __ldg(img4 + o0);
+        const float4 pb4 = __ldg(img4 + (two ? o0 + stp : o0));
+        const float mb = two ? 1.0f : 0.0f;  // a masked second candidate adds zeros
+        const float2 a01 = make_float2(pa4.x, pa4.y), a23 = make_float2(pa4.z, pa4.w);
+        const float2 mb2 = make_float2(mb, mb);
+        const float2 b01 = __fmul2_rn(make_float2(pb4.x, pb4.y), mb2);
+        const float2 b23 = __fmul2_rn(make_float2(pb4.z, pb4.w), mb2);
+#pragma unroll
+        for (int q = 0; q < kRayGroup; ++q) {
+          const float wa = fmaxf(0.0f, 1.0f - fabsf(pos - (float)q));
+          const float wb = fmaxf(0.0f, 1.0f - fabsf(pb - (float)q));
+          const float2 wa2 = make_float2(wa, wa), wb2 = make_float2(wb, wb);
+          acc01[q] = __ffma2_rn(wb2, b01, __ffma2_rn(wa2, a01, acc01[q]));
+          acc23[q] = __ffma2_rn(wb2, b23, __ffma2_rn(wa2, a23, acc23[q]));
+        }
+        o0 += 2 * stp;
+        pos = pb + Y;
+      }
+    }
+  }
+  float acc[kOrbit][kRayGroup];
+#pragma unroll
+  for (int q = 0; q < kRayGroup; ++q) {
+    acc[0][q] = acc01[q].x;
+    acc[1][q] = acc01[q].y;
+    acc[2][q] = acc23[q].x;
+    acc[3][q] = acc23[q].y;
+  }
+  if (SPLIT > 1) {
+#pragma unroll
+    for (int m = 0; m < kOrbit; ++m) warp_reduce_rows<SPLIT>(acc[m]);
+  }
+  double part = 0.0;
+  if (active && L.lane_group == 0) {
+    const float scale = g.delta_x * g.delta_x / g.delta_xi;
+    const int64_t mirror_max = d.Ns - 1 - H;  // mirrored outputs for s <= this
+#pragma unroll
+    for (int q = 0; q < kRayGroup; ++q) {
+      const int64_t s = s0 + q;
+      if (s < H) {
+#pragma unroll
+        for (int m = 0; m < kOrbit; ++m) {
+          const int c = (m + shift) & (kOrbit - 1);
+          if ((c & 2) && s > mirror_max) continue;
+          const int64_t bin = (c & 2) ? d.Ns - 1 - s : s;
+          const int64_t ang = k + ((c & 1) ? Q : 0);
+          part += epi(bin, ang, 0, sino_index<SO>(bin, ang, 0, d), acc[m][q] * scale);
+        }
+      }
+    }
+  }
+  return part;
+}
+
+template <int SO, int SPLIT, class Epi>
+__global__ void __launch_bounds__(kFwdBlock)
+radon_fwd_quarter(const float4* __restrict__ img4, const float* __restrict__ ofs,
+                  RadonGeo<float> g, Dims d, Epi epi, double* __restrict__ partials,
+                  const int* __restrict__ skip) {
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const double part = radon_fwd_quarter_tile<SO, SPLIT, Epi>(img4, ofs, g, d, epi, blockIdx);
+  if (Epi::kReduce) {
+    const double t = block_sum(part, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
+  }
+}
+
+// Row copy of the parallel-beam orbits: for base angle k < Q, entry 1 + j
+// holds (row_k[j], row_{k+Q}[j], row_k[Ns-1-j], row_{k+Q}[Ns-1-j]), j = -1
+// .. Ns + 1 (zeros off the detector).  Interpolating an entry pair at a
+// position u gives the two rows at u and, in the last two lanes, the two
+// rows at the mirrored position Ns - 1 - u, with the same weights.
+template <int SO>
+__global__ void __launch_bounds__(256)
+radon_orbit_rows(const float* __restrict__ sino, Dims d, float4* __restrict__ rows4,
+                 const int* __restrict__ skip) {
+  if (skip != nullptr && *skip) return;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = blockIdx.y;
+  const int64_t nrow = d.Ns + kOrbitRowPad;
+  if (e >= nrow) return;
+  const int64_t Q = d.Na / 2;
+  int64_t ss_, sa_, sz_;
+  sino_strides<SO>(d, ss_, sa_, sz_);
+  const int64_t j = e - 1, jm = d.Ns - 1 - j;
+  auto at = [&](int64_t s, int64_t a) {
+    return (s >= 0 && s < d.Ns) ? ldg(sino + s * ss_ + a * sa_) : 0.0f;
+  };
+  rows4[k * nrow + e] = make_float4(at(j, k), at(j, k + Q), at(jm, k), at(jm, k + Q));
+}
+
+// Backprojection over the parallel-beam orbits from radon_orbit_rows: a
+// thread owns the orbit P0, P1 = S P0, P2 = -P0, P3 = -S P0 of one pixel of
+// the quadrant x, y < N/2 (N even); for base angle k it evaluates the
+// detector positions u0 of P0 and u1 of P1 (those of P2 and P3 are their
+// mirrors) and, with one entry pair per position, adds 8 pixel-angles:
+//   u0: (P0, k) (P3, k+Q) (P2, k) (P1, k+Q)   u1: (P1, k) (P0, k+Q) (P3, k) (P2, k+Q)
+// (xi(k + Q, P) = xi(k, S P) and xi(k, -P) = Ns - 1 - xi(k, P)).  The row
+// values are interpolated as v0 + fr (v1 - v0) and weighted by the angle's
+// weight, as radon.cl:183-241 does; G thread groups take interleaved base
+// angles and are added in a fixed order.
+template <int IO, int G, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__ ofs, Dims d,
+                     QuarterMaps qm, Epi epi, double* __restrict__ partials,
+                     const int* __restrict__ skip) {
+  constexpr int kOrbit = 4;
+  constexpr int kRowsT = kBwdTileSlow / G;
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const int lane = threadIdx.x, trow = threadIdx.y;
+  const int grp = trow / kRowsT, trow_t = trow % kRowsT;
+  const int N = (int)d.Nx, half = N / 2;
+  const int Q = (int)(d.Na / 2);
+  const int nrow = (int)d.Ns + kOrbitRowPad;
+  const int px0 = (int)blockIdx.x * kBwdTileFast + lane;
+  const int py0 = (int)blockIdx.y * kRowsT + trow_t;
+  const bool own = px0 < half && py0 < half;
+  // S is the transpose of the first lookup map S^-1
+  auto orbit = [&](int (&ox)[kOrbit], int (&oy)[kOrbit]) {
+    const int c2 = N - 1;  // twice the centre
+    const int dx = 2 * px0 - c2, dy = 2 * py0 - c2;  // twice P0 - centre
+    const int sx = qm.axx[0] * dx + qm.ayx[0] * dy, sy = qm.axy[0] * dx + qm.ayy[0] * dy;
+    ox[0] = px0;
+    oy[0] = py0;
+    ox[1] = (c2 + sx) / 2;
+    oy[1] = (c2 + sy) / 2;
+    ox[2] = c2 - px0;
+    oy[2] = c2 - py0;
+    ox[3] = c2 - ox[1];
+    oy[3] = c2 - oy[1];
+  };
+  float2 pxr, pyr;  // P0 and P1 relative to the image centre
+  {
+    int ox[kOrbit], oy[kOrbit];
+    orbit(ox, oy);
+    const float c = 0.5f * (float)(N - 1);
+    pxr = make_float2((float)ox[0] - c, (float)ox[1] - c);
+    pyr = make_float2((float)oy[0] - c, (float)oy[1] - c);
+  }
+  const float mid1 = 0.5f * (float)(d.Ns - 1) + 1.0f;  // padded entry of the centre
+  const float2 mid2 = make_float2(mid1, mid1);
+  const float hi = (float)d.Ns + 1.0f;
+  const float2 neg = make_float2(-1.0f, -1.0f);
+  // (P0, P3) (P2, P1) (P1, P0) (P3, P2)
+  float2 A = make_float2(0.f, 0.f), B = A, C = A, D = A;
+  for (int k = grp; k < Q; k += G) {
+    const float X = ldg(ofs + 8 * k), Y = ldg(ofs + 8 * k + 1);
+    const float2 W = make_float2(ldg(ofs + 8 * k + 4), ldg(ofs + 8 * (k + Q) + 4));
+    const float2 u = __ffma2_rn(make_float2(X, X), pxr, __ffma2_rn(make_float2(Y, Y), pyr, mid2));
+    const float uc[2] = {fminf(fmaxf(u.x, 0.0f), hi), fminf(fmaxf(u.y, 0.0f), hi)};
+    const float4* row = rows4 + k * nrow;
+    float2 lo[2], hi2[2];
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const float fl = floorf(uc[e]);
+      const float fr = uc[e] - fl;
+      const int n = (int)fl;
+      const float4 e0 = __ldg(row + n), e1 = __ldg(row + n + 1);
+      const float2 f2 = make_float2(fr, fr);
+      const float2 l0 = make_float2(e0.x, e0.y), h0 = make_float2(e0.z, e0.w);
+      lo[e] = __ffma2_rn(f2, __ffma2_rn(l0, neg, make_float2(e1.x, e1.y)), l0);
+      hi2[e] = __ffma2_rn(f2, __ffma2_rn(h0, neg, make_float2(e1.z, e1.w)), h0);
+    }
+    A = __ffma2_rn(W, lo[0], A);
+    B = __ffma2_rn(W, hi2[0], B);
+    C = __ffma2_rn(W, lo[1], C);
+    D = __ffma2_rn(W, hi2[1], D);
+  }
+  float sum[kOrbit] = {A.x + C.y, B.y + C.x, B.x + D.y, A.y + D.x};
+  if constexpr (G > 1) {
+    __shared__ float cred[kBwdTileSlow][kOrbit][kBwdTileFast];
+#pragma unroll
+    for (int m = 0; m < kOrbit; ++m) cred[trow][m][lane] = sum[m];
+    __syncthreads();
+    if (grp == 0) {
+#pragma unroll
+      for (int m = 0; m < kOrbit; ++m) {
+        float t = cred[trow][m][lane];
+#pragma unroll
+        for (int q = 1; q < G; ++q) t += cred[trow + q * kRowsT][m][lane];
+        sum[m] = t;
+      }
+    }
+  }
+  double part = 0.0;
+  if (own && grp == 0) {
+    int ox[kOrbit], oy[kOrbit];
+    orbit(ox, oy);
+#pragma unroll
+    for (int m = 0; m < kOrbit; ++m)
+      part += epi(ox[m], oy[m], 0, img_index<IO>(ox[m], oy[m], 0, d), sum[m]);
   }
   if (Epi::kReduce) {
     const double t = block_sum(part, red);

@@ -83,3 +83,64 @@ def fan_quarter_maps(struct, img_shape, atol_bins: float = 1e-6, rtol_t: float =
         Cy = int(round(c * (1 - Ayx - Ayy)))
         maps.append((Axx, Axy, Ayx, Ayy, Cx, Cy))
     return maps
+
+
+def radon_half_maps(struct, img_shape, atol_bins: float = 1e-6):
+    """Index maps of the quarter-turn-and-mirror orbit of a parallel-beam
+    geometry, or None.
+
+    With a square image centred on the rotation axis, a detector centred on
+    the central ray and Na angles equispaced over [0, pi) (Na even), angle
+    k + Na/2 sees the grid as angle k sees it after a quarter turn S, and
+    angle k sees the grid turned by a half as its own detector reversed
+    (bin s <-> Ns - 1 - s; p(-s, phi) = p(s, phi + pi)).  For a base angle
+    k < Na/2 and a bin s the four outputs
+
+        (s, k), (s, k + Na/2), (Ns-1-s, k), (Ns-1-s, k + Na/2)
+
+    are then sums of the weights of angle k applied to img(P), img(S^-1 P),
+    img(-P) and img(-S^-1 P).  Returned in the format of
+    :func:`fan_quarter_maps`: three tuples ``(Axx, Axy, Ayx, Ayy, Cx, Cy)``
+    for those three lookups, or None when a check fails (the detector
+    coordinate xi = X x + Y y + offset of radon.cl:183-241 is evaluated in
+    float64 on sample pixels for every base angle).
+    """
+    Nx, Ny = (int(v) for v in img_shape)
+    ofs = np.asarray(struct["ofs_dict"][np.dtype("float64")], dtype=np.float64)
+    geo = np.asarray(struct["geo_dict"][np.dtype("float64")], dtype=np.float64)
+    Na = ofs.shape[1]
+    if Nx != Ny or Na < 2 or Na % 2 != 0:
+        return None
+    Ns = int(round(geo[4]))
+    c = (Nx - 1) * 0.5
+    mid = (Ns - 1) * 0.5
+    X, Y, off = ofs[0], ofs[1], ofs[2]
+    # the image centre projects onto the detector centre at every angle
+    if not np.all(np.abs(X * c + Y * c + off - mid) <= atol_bins):
+        return None
+    Q = Na // 2
+    px, py = _sample_pixels(Nx)
+    px, py = px - c, py - c
+
+    def xi(a, Xr, Yr):
+        return X[a][:, None] * Xr + Y[a][:, None] * Yr + mid
+
+    base = np.arange(Q)
+    x1 = xi(base + Q, px[None, :], py[None, :])
+    found = None
+    for S in _MAPS[2:4]:  # the two quarter turns
+        Xr = S[0] * px + S[1] * py
+        Yr = S[2] * px + S[3] * py
+        if np.all(np.abs(x1 - xi(base, Xr[None, :], Yr[None, :])) <= atol_bins):
+            found = S
+            break
+    if found is None:
+        return None
+    # lookups: S^-1 = S^T, then -I, then -S^-1
+    inv = (found[0], found[2], found[1], found[3])
+    maps = []
+    for A in (inv, (-1, 0, 0, -1), tuple(-v for v in inv)):
+        Cx = int(round(c * (1 - A[0] - A[1])))
+        Cy = int(round(c * (1 - A[2] - A[3])))
+        maps.append((A[0], A[1], A[2], A[3], Cx, Cy))
+    return maps

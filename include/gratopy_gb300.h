@@ -68,7 +68,14 @@ typedef struct gr_geometry {
    * cy): pixel (x, y) of angle a is pixel (cx + axx x + axy y, cy + ayx x +
    * ayy y) of angle a + m*Na/4.  The float32 fan-beam forward projection of
    * single slices then shares each pixel's interpolation weights across the
-   * four angles.  Set by the Python layer after checking the geometry. */
+   * four angles.  2 for a parallel-beam geometry with Na angles equispaced
+   * over [0, pi) (Na even), a centred square image and a centred detector:
+   * sym_map[0..2] are then the lookups S^-1, -I, -S^-1 (S the quarter turn
+   * with which angle k + Na/2 sees the grid as angle k does) that give the
+   * outputs (s, k + Na/2), (Ns-1-s, k), (Ns-1-s, k + Na/2) from the weights
+   * of angle k; the float32 projections of single slices then run over these
+   * orbits when `work` holds their copies.  Set by the Python layer after
+   * checking the geometry. */
   int sym;
   int sym_map[3][6];
   /* Device scratch (no counterpart in the reference) that a call may use

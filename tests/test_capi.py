@@ -143,6 +143,34 @@ def test_host_only_entry_points(library):
     assert bwd_parts(ctypes.byref(q), 3, 0) == 16 * 512 * 3
     q.fwd_split = q.bwd_split = 0
     assert lib.gr_forward_partials(None, 1) == 0
+    # parallel beam with the half-circle orbit maps (sym = 2): accepted for
+    # Radon only; the orbit kernels run when the scratch holds their copies
+    # (the forward's float4 per pixel, the backprojection's mirror-interleaved
+    # rows: Ns + 3 float4 per base angle), with grids over the bins
+    # s < ceil(Ns/2) and base angles k < Na/2 (two per block, 4 * fwd_split
+    # lanes per group) for the forward and over the quadrant for the
+    # backprojection
+    r = _lib.GrGeometry()
+    r.kind, r.dtype, r.Nx, r.Ny, r.Ns, r.Na = 0, 0, 256, 256, 363, 180
+    r.ofs = fake
+    r.sym = 2
+    for m, row in enumerate([(0, -1, 1, 0, 255, 0), (-1, 0, 0, -1, 255, 255),
+                             (0, 1, -1, 0, 0, 255)]):
+        for k, v in enumerate(row):
+            r.sym_map[m][k] = v
+    need = work(ctypes.byref(r), 1)
+    assert need == max(256 * 256 * 16, 90 * (363 + 3) * 16)
+    assert work(ctypes.byref(r), 2) == 0  # single slices only
+    r.fwd_split, r.bwd_split = 8, 8
+    no_work = fwd_parts(ctypes.byref(r), 1)
+    assert no_work == -(-363 // 32) * 180  # per-angle forward, 16 lanes per group
+    r.work, r.work_bytes = ctypes.c_void_p(1 << 20), need
+    assert fwd_parts(ctypes.byref(r), 1) == -(-182 // 8) * 45  # 32 lanes per group
+    assert bwd_parts(ctypes.byref(r), 1, 0) == 4 * 128
+    r.work_bytes = 256 * 256 * 16 - 16  # too small for the forward's copy
+    assert fwd_parts(ctypes.byref(r), 1) == no_work
+    r.kind, r.sdpd = 1, fake  # sym = 2 is for parallel beam only
+    assert lib.gr_forward(ctypes.byref(r), fake, fake, 1, 0, 0, None) == 1
     # descriptors: binding layouts equal the library's
     assert lib.gr_geometry_size() == ctypes.sizeof(_lib.GrGeometry)
     assert lib.gr_batch_problem_size() == ctypes.sizeof(_lib.GrBatchProblem)

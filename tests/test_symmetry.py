@@ -51,3 +51,53 @@ def test_maps_turn_the_image_between_quarter_angles(name):
 def test_asymmetric_geometries_are_rejected(name):
     ps = host_settings(dict(BASE, **ASYMMETRIC[name]))
     assert fan_quarter_maps(ps.struct, ps.img_shape) is None
+
+
+# parallel beam: the half-circle orbits (quarter turn and detector mirror)
+RADON_BASE = dict(geometry="radon", img_shape=(40, 40), angles=30, n_detectors=57)
+RADON_SYMMETRIC = {
+    "plain": {},
+    "odd_side_odd_detectors": dict(img_shape=(37, 37), angles=18, n_detectors=53),
+    "even_detectors": dict(n_detectors=60),
+    "wide_detector": dict(detector_width=3.0, image_width=2.0),
+    "bench_256": dict(img_shape=(256, 256), angles=180, n_detectors=363,
+                      detector_width=2.0 * np.sqrt(2.0)),
+}
+RADON_ASYMMETRIC = {
+    "not_square": dict(img_shape=(40, 36)),
+    "odd_angle_count": dict(angles=31),
+    "shifted_detector": dict(detector_shift=0.01),
+    "shifted_image": dict(midpoint_shift=(0.02, 0.0)),
+    "limited_range": dict(angles=[(30, 0.0, 2.0)]),
+}
+
+
+@pytest.mark.parametrize("name", sorted(RADON_SYMMETRIC))
+def test_radon_maps_give_the_four_outputs(name):
+    """The oracle's projection of the image looked up through map m, at the
+    base angles k < Na/2, equals the outputs (s, k + Na/2), (Ns-1-s, k),
+    (Ns-1-s, k + Na/2) of the original image (float64, 1e-12)."""
+    from gratopy_gb300.symmetry import radon_half_maps
+
+    ps = host_settings(dict(RADON_BASE, **RADON_SYMMETRIC[name]))
+    maps = radon_half_maps(ps.struct, ps.img_shape)
+    assert maps is not None
+    N = ps.img_shape[0]
+    Ns, Na = ps.sinogram_shape
+    Q = Na // 2
+    img = np.asfortranarray(np.random.default_rng(4).random((N, N)))
+    ref = O.forward(img, ps)
+    x, y = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
+    want = {1: ref[:, Q:], 2: ref[::-1, :Q], 3: ref[::-1, Q:]}
+    for m, (axx, axy, ayx, ayy, cx, cy) in enumerate(maps, start=1):
+        turned = np.asfortranarray(img[cx + axx * x + axy * y, cy + ayx * x + ayy * y])
+        got = O.forward(turned, ps)[:, :Q]
+        assert np.abs(got - want[m]).max() <= 1e-12 * np.abs(want[m]).max(), m
+
+
+@pytest.mark.parametrize("name", sorted(RADON_ASYMMETRIC))
+def test_radon_asymmetric_geometries_are_rejected(name):
+    from gratopy_gb300.symmetry import radon_half_maps
+
+    ps = host_settings(dict(RADON_BASE, **RADON_ASYMMETRIC[name]))
+    assert radon_half_maps(ps.struct, ps.img_shape) is None
