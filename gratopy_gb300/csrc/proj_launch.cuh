@@ -223,30 +223,42 @@ inline size_t quarter_bwd_bytes(const gr_geometry* g, int Nz) {
          sizeof(float4);
 }
 
-// Parallel beam, float32 single slices with the half-circle orbit maps
-// (sym = 2): the orbit kernels read copies of the image (the forward, any
-// side) and of the sinogram (the backprojection, even sides), so each runs
-// only when the caller's scratch holds its copy; otherwise the per-angle
-// kernels run.
+// Stacks take the parallel-beam orbit forward slice by slice from this many
+// pixel-angles per slice, and never the orbit backprojection: the 4-slice
+// per-angle kernels share each pixel-angle's geometry over 4 slices instead
+// (measured with a one-slice scratch, Gpixel-angle/s forward / back:
+// 256^2 x 180 x 16 orbit 615 / 698, per-angle 829 / 1593; 512^2 x 360 x 16
+// orbit 1448 / 1749, per-angle 919 / 2020; 1024^2 x 720 x 4 orbit 2004 /
+// 2021, per-angle 901 / 2055).
+constexpr int64_t kRadonOrbitStackMin = 32ll << 20;
+
+// Parallel beam, float32 with the half-circle orbit maps (sym = 2): the orbit
+// kernels read copies of the image (the forward, any side) and of the
+// sinogram (the backprojection, even sides), so each runs only when the
+// caller's scratch holds its copy of a slice; otherwise the per-angle kernels
+// run.
 inline bool use_radon_orbit(const gr_geometry* g, int Nz) {
-  return g->sym == 2 && g->dtype == GR_F32 && g->kind == GR_RADON && Nz == 1 &&
-         g->Na % 2 == 0 && g->Nx == g->Ny && (int64_t)g->Nx * g->Ny <= INT32_MAX &&
+  return g->sym == 2 && g->dtype == GR_F32 && g->kind == GR_RADON && Nz >= 1 &&
+         Nz <= 65535 && g->Na % 2 == 0 && g->Nx == g->Ny &&
+         (int64_t)g->Nx * g->Ny <= INT32_MAX &&
          (int64_t)(g->Ns + fast::kOrbitRowPad) * (g->Na / 2) <= INT32_MAX;
 }
 
 inline size_t radon_orbit_fwd_bytes(const gr_geometry* g, int Nz) {
-  return use_radon_orbit(g, Nz) ? (size_t)g->Nx * (size_t)g->Ny * sizeof(float4) : 0;
+  if (!use_radon_orbit(g, Nz) || (Nz > 1 && pixel_angles(g) < kRadonOrbitStackMin)) return 0;
+  return (size_t)g->Nx * (size_t)g->Ny * sizeof(float4);
 }
 
 inline size_t radon_orbit_bwd_bytes(const gr_geometry* g, int Nz) {
-  if (!use_radon_orbit(g, Nz) || g->Nx % 2 != 0) return 0;
+  if (!use_radon_orbit(g, Nz) || Nz != 1 || g->Nx % 2 != 0) return 0;
   return (size_t)(g->Na / 2) * (size_t)(g->Ns + fast::kOrbitRowPad) * sizeof(float4);
 }
 
 inline size_t orbit_work_bytes(const gr_geometry* g, int Nz) {
   if (g->kind == GR_RADON) {
     const size_t f = radon_orbit_fwd_bytes(g, Nz), b = radon_orbit_bwd_bytes(g, Nz);
-    return f > b ? f : b;
+    const int slices = Nz < kQuarterCopySlices ? Nz : kQuarterCopySlices;
+    return (f > b ? f : b) * (size_t)(slices > 0 ? slices : 0);
   }
   const size_t f = quarter_fwd_bytes(g, Nz), b = quarter_bwd_bytes(g, Nz);
   const int slices = Nz < kQuarterCopySlices ? Nz : kQuarterCopySlices;
@@ -264,12 +276,11 @@ inline int work_slices(const gr_geometry* g, size_t per_slice, int Nz) {
 
 
 inline bool use_radon_orbit_fwd(const gr_geometry* g, int Nz) {
-  return use_radon_orbit(g, Nz) && work_slices(g, radon_orbit_fwd_bytes(g, Nz), Nz) > 0;
+  return work_slices(g, radon_orbit_fwd_bytes(g, Nz), Nz) > 0;
 }
 
 inline bool use_radon_orbit_bwd(const gr_geometry* g, int Nz) {
-  return g->Nx % 2 == 0 && use_radon_orbit(g, Nz) &&
-         work_slices(g, radon_orbit_bwd_bytes(g, Nz), Nz) > 0;
+  return work_slices(g, radon_orbit_bwd_bytes(g, Nz), Nz) > 0;
 }
 
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
@@ -285,7 +296,7 @@ inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
     const int apb = fast::kQuarterAnglesPerBlock;
     const int qb = (32 / (4 * split)) * (kFwdBlock / 32 / apb) * group;  // 4 * split lanes
     const int H = (int)((g->Ns + 1) / 2);
-    return dim3((H + qb - 1) / qb, (g->Na / 2 + apb - 1) / apb, 1);
+    return dim3((H + qb - 1) / qb, (g->Na / 2 + apb - 1) / apb, Nz);  // one launch per slice
   }
   if (g->dtype == GR_F32 && g->kind == GR_RADON && Nz == 1) {  // 2 * split lanes per group
     const int rb = (32 / (2 * split)) * (kFwdBlock / 32) * group;
@@ -328,29 +339,40 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
   const dim3 grid = fwd_grid(g, Nz, SPLIT);
   if constexpr (std::is_same<T, float>::value) {
     if (g->kind == GR_RADON) {
-      if constexpr (ZB == 1) {
-        if (use_radon_orbit_fwd(g, Nz)) {
-          // half-circle orbits: each pixel's four orbit pixels as one float4,
-          // then the forward over the orbits
-          const fast::QuarterMaps qm = quarter_maps(g);
-          float4* img4 = static_cast<float4*>(g->work);
+      if (use_radon_orbit_fwd(g, Nz)) {
+        // half-circle orbits, slices in chunks: each pixel's four orbit pixels
+        // as one float4, then the forward over the orbits, one launch per
+        // slice (each launch's block partials follow the previous slice's)
+        const fast::QuarterMaps qm = quarter_maps(g);
+        float4* img4 = static_cast<float4*>(g->work);
+        const int chunk = work_slices(g, radon_orbit_fwd_bytes(g, Nz), Nz);
+        const int64_t slice4 = (int64_t)g->Nx * g->Ny;
+        const dim3 sgrid(grid.x, grid.y, 1);
+        const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
+        for (int z0 = 0; z0 < Nz; z0 += chunk) {
+          const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;
           if constexpr (IO == ORDER_F) {
             constexpr int kTile = fast::kOrbitTile;
-            const dim3 tgrid((g->Nx + kTile - 1) / kTile, (g->Ny + kTile - 1) / kTile, 1);
+            const dim3 tgrid((g->Nx + kTile - 1) / kTile, (g->Ny + kTile - 1) / kTile, zc);
             fast::orbit_pixels_tiled<IO><<<tgrid, dim3(kTile, kTile), 0, st>>>(img, d, qm, img4,
-                                                                               0, skip);
+                                                                               z0, skip);
           } else {
-            const dim3 pgrid((g->Nx + 255) / 256, g->Ny, 1);
-            fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, 0, skip);
+            const dim3 pgrid((g->Nx + 255) / 256, g->Ny, zc);
+            fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, z0, skip);
           }
           // four times the lanes per group: a group's work is shared by four
           // outputs, so the orbit forward has a quarter of the groups (256^2 x
-          // 180: 16 lanes 41.6 us, 8 lanes 63.4 us)
-          fast::radon_fwd_quarter<SO, 4 * SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
-              img4, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo), d, epi,
-              partials, skip);
-          return check_launch();
+          // 180: 16 lanes 41.6 us, 8 lanes 63.4 us, 32 lanes 29.8 us)
+          for (int c = 0; c < zc; ++c) {
+            const int64_t z = z0 + c;
+            fast::radon_fwd_quarter<SO, 4 * SPLIT, Epi><<<sgrid, kFwdBlock, 0, st>>>(
+                img4 + c * slice4, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo),
+                d, epi, partials ? partials + z * per_slice_blocks : nullptr, skip, z);
+          }
         }
+        return check_launch();
+      }
+      if constexpr (ZB == 1) {
         // single slices run twice the lanes per bin group (fwd_grid): one
         // Radon slice is too small to fill the GPU with SPLIT lanes
         fast::radon_fwd_fast<SO, IO, 1, 2 * SPLIT, Epi><<<grid, kFwdBlock, 0, st>>>(
@@ -488,13 +510,19 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
             sino, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials, skip, 0);
       }
     } else if (use_radon_orbit_bwd(g, Nz)) {
-      // half-circle orbits: the mirror-interleaved row copy, then the
-      // backprojection over the orbits
+      // half-circle orbits, slices in chunks: the mirror-interleaved row
+      // copies, then the backprojection over the orbits (one slice per block)
       float4* rows4 = static_cast<float4*>(g->work);
-      const dim3 rgrid((g->Ns + fast::kOrbitRowPad + 255) / 256, g->Na / 2, 1);
-      fast::radon_orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, d, rows4, skip);
-      fast::radon_bwd_orbit_rows<IO, SPLIT, Epi><<<grid, block, 0, st>>>(
-          rows4, static_cast<const float*>(g->ofs), d, quarter_maps(g), epi, partials, skip);
+      const int chunk = work_slices(g, radon_orbit_bwd_bytes(g, Nz), Nz);
+      const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
+      for (int z0 = 0; z0 < Nz; z0 += chunk) {
+        const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;
+        const dim3 rgrid((g->Ns + fast::kOrbitRowPad + 255) / 256, g->Na / 2, zc);
+        fast::radon_orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, d, rows4, z0, skip);
+        fast::radon_bwd_orbit_rows<IO, SPLIT, Epi><<<dim3(grid.x, grid.y, zc), block, 0, st>>>(
+            rows4, static_cast<const float*>(g->ofs), d, quarter_maps(g), epi,
+            partials ? partials + z0 * per_slice_blocks : nullptr, skip, z0);
+      }
     } else if (g->kind == GR_RADON) {
       fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, fblock, 0, st>>>(
           sino, static_cast<const float*>(g->ofs), d, epi, partials, skip);

@@ -1487,7 +1487,7 @@ template <int SO, int SPLIT, class Epi>
 __device__ __forceinline__ double radon_fwd_quarter_tile(const float4* __restrict__ img4,
                                                          const float* __restrict__ ofs,
                                                          RadonGeo<float> g, Dims d, Epi epi,
-                                                         uint3 bid) {
+                                                         uint3 bid, int64_t z) {
   constexpr int kOrbit = 4;
   const QuarterLayout<SPLIT> L(bid);
   const int64_t s0 = L.s0;
@@ -1573,7 +1573,7 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float4* __restric
           if ((c & 2) && s > mirror_max) continue;
           const int64_t bin = (c & 2) ? d.Ns - 1 - s : s;
           const int64_t ang = k + ((c & 1) ? Q : 0);
-          part += epi(bin, ang, 0, sino_index<SO>(bin, ang, 0, d), acc[m][q] * scale);
+          part += epi(bin, ang, z, sino_index<SO>(bin, ang, z, d), acc[m][q] * scale);
         }
       }
     }
@@ -1581,14 +1581,15 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float4* __restric
   return part;
 }
 
+// One launch per slice: img4 points at slice z's orbit copy.
 template <int SO, int SPLIT, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
 radon_fwd_quarter(const float4* __restrict__ img4, const float* __restrict__ ofs,
                   RadonGeo<float> g, Dims d, Epi epi, double* __restrict__ partials,
-                  const int* __restrict__ skip) {
+                  const int* __restrict__ skip, int64_t z) {
   __shared__ double red[32];
   if (skip != nullptr && *skip) return;
-  const double part = radon_fwd_quarter_tile<SO, SPLIT, Epi>(img4, ofs, g, d, epi, blockIdx);
+  const double part = radon_fwd_quarter_tile<SO, SPLIT, Epi>(img4, ofs, g, d, epi, blockIdx, z);
   if (Epi::kReduce) {
     const double t = block_sum(part, red);
     if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
@@ -1599,10 +1600,11 @@ radon_fwd_quarter(const float4* __restrict__ img4, const float* __restrict__ ofs
 // holds (row_k[j], row_{k+Q}[j], row_k[Ns-1-j], row_{k+Q}[Ns-1-j]), j = -1
 // .. Ns + 1 (zeros off the detector).  Interpolating an entry pair at a
 // position u gives the two rows at u and, in the last two lanes, the two
-// rows at the mirrored position Ns - 1 - u, with the same weights.
+// rows at the mirrored position Ns - 1 - u, with the same weights.  Slice
+// z0 + blockIdx.z goes to copy blockIdx.z.
 template <int SO>
 __global__ void __launch_bounds__(256)
-radon_orbit_rows(const float* __restrict__ sino, Dims d, float4* __restrict__ rows4,
+radon_orbit_rows(const float* __restrict__ sino, Dims d, float4* __restrict__ rows4, int64_t z0,
                  const int* __restrict__ skip) {
   if (skip != nullptr && *skip) return;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1612,11 +1614,13 @@ radon_orbit_rows(const float* __restrict__ sino, Dims d, float4* __restrict__ ro
   const int64_t Q = d.Na / 2;
   int64_t ss_, sa_, sz_;
   sino_strides<SO>(d, ss_, sa_, sz_);
+  const float* slice = sino + (z0 + blockIdx.z) * sz_;
   const int64_t j = e - 1, jm = d.Ns - 1 - j;
   auto at = [&](int64_t s, int64_t a) {
-    return (s >= 0 && s < d.Ns) ? ldg(sino + s * ss_ + a * sa_) : 0.0f;
+    return (s >= 0 && s < d.Ns) ? ldg(slice + s * ss_ + a * sa_) : 0.0f;
   };
-  rows4[k * nrow + e] = make_float4(at(j, k), at(j, k + Q), at(jm, k), at(jm, k + Q));
+  rows4[((int64_t)blockIdx.z * Q + k) * nrow + e] =
+      make_float4(at(j, k), at(j, k + Q), at(jm, k), at(jm, k + Q));
 }
 
 // Backprojection over the parallel-beam orbits from radon_orbit_rows: a
@@ -1633,7 +1637,7 @@ template <int IO, int G, class Epi>
 __global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
 radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__ ofs, Dims d,
                      QuarterMaps qm, Epi epi, double* __restrict__ partials,
-                     const int* __restrict__ skip) {
+                     const int* __restrict__ skip, int64_t z0) {
   constexpr int kOrbit = 4;
   constexpr int kRowsT = kBwdTileSlow / G;
   __shared__ double red[32];
@@ -1672,6 +1676,8 @@ radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__
   const float2 mid2 = make_float2(mid1, mid1);
   const float hi = (float)d.Ns + 1.0f;
   const float2 neg = make_float2(-1.0f, -1.0f);
+  const int64_t z = z0 + blockIdx.z;  // slice; its copy is copy blockIdx.z
+  rows4 += (int64_t)blockIdx.z * Q * nrow;
   // (P0, P3) (P2, P1) (P1, P0) (P3, P2)
   float2 A = make_float2(0.f, 0.f), B = A, C = A, D = A;
   for (int k = grp; k < Q; k += G) {
@@ -1719,7 +1725,7 @@ radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__
     orbit(ox, oy);
 #pragma unroll
     for (int m = 0; m < kOrbit; ++m)
-      part += epi(ox[m], oy[m], 0, img_index<IO>(ox[m], oy[m], 0, d), sum[m]);
+      part += epi(ox[m], oy[m], z, img_index<IO>(ox[m], oy[m], z, d), sum[m]);
   }
   if (Epi::kReduce) {
     const double t = block_sum(part, red);

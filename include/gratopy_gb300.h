@@ -74,8 +74,9 @@ typedef struct gr_geometry {
    * with which angle k + Na/2 sees the grid as angle k does) that give the
    * outputs (s, k + Na/2), (Ns-1-s, k), (Ns-1-s, k + Na/2) from the weights
    * of angle k; the float32 projections of single slices then run over these
-   * orbits when `work` holds their copies.  Set by the Python layer after
-   * checking the geometry. */
+   * orbits when `work` holds their copies, and so does the forward projection
+   * of stacks from 32 * 2^20 pixel-angles per slice, slice by slice.  Set by
+   * the Python layer after checking the geometry. */
   int sym;
   int sym_map[3][6];
   /* Device scratch (no counterpart in the reference) that a call may use

@@ -160,7 +160,7 @@ def test_host_only_entry_points(library):
             r.sym_map[m][k] = v
     need = work(ctypes.byref(r), 1)
     assert need == max(256 * 256 * 16, 90 * (363 + 3) * 16)
-    assert work(ctypes.byref(r), 2) == 0  # single slices only
+    assert work(ctypes.byref(r), 2) == 0  # stacks of slices below 32 * 2^20 pixel-angles
     r.fwd_split, r.bwd_split = 8, 8
     no_work = fwd_parts(ctypes.byref(r), 1)
     assert no_work == -(-363 // 32) * 180  # per-angle forward, 16 lanes per group
@@ -169,6 +169,22 @@ def test_host_only_entry_points(library):
     assert bwd_parts(ctypes.byref(r), 1, 0) == 4 * 128
     r.work_bytes = 256 * 256 * 16 - 16  # too small for the forward's copy
     assert fwd_parts(ctypes.byref(r), 1) == no_work
+    # stacks of larger slices: the orbit forward slice by slice (one slice's
+    # copy per slice, up to 8 per launch pair), the per-angle backprojection
+    r.Nx = r.Ny = 512
+    r.Ns, r.Na = 725, 360
+    for m, row in enumerate([(0, -1, 1, 0, 511, 0), (-1, 0, 0, -1, 511, 511),
+                             (0, 1, -1, 0, 0, 511)]):
+        for k, v in enumerate(row):
+            r.sym_map[m][k] = v
+    assert work(ctypes.byref(r), 3) == 3 * 512 * 512 * 16
+    assert work(ctypes.byref(r), 20) == 8 * 512 * 512 * 16
+    r.work_bytes = 512 * 512 * 16
+    assert fwd_parts(ctypes.byref(r), 3) == -(-363 // 8) * 90 * 3
+    per_angle_bwd = bwd_parts(ctypes.byref(r), 3, 0)
+    r.sym = 0
+    assert bwd_parts(ctypes.byref(r), 3, 0) == per_angle_bwd
+    r.sym = 2
     r.kind, r.sdpd = 1, fake  # sym = 2 is for parallel beam only
     assert lib.gr_forward(ctypes.byref(r), fake, fake, 1, 0, 0, None) == 1
     # descriptors: binding layouts equal the library's

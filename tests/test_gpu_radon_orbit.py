@@ -1,4 +1,4 @@
-"""Parallel-beam projections over half-circle orbits (float32 single slices).
+"""Parallel-beam projections over half-circle orbits (float32).
 
 For angles equispaced over [0, pi) with Na even, a centred square image and
 a centred detector, the forward projection shares each candidate pixel's
@@ -7,7 +7,9 @@ weights over the four outputs (s, k), (s, k + Na/2), (Ns-1-s, k),
 over the eight pixel-angles of a pixel orbit.  Checked against the float64
 oracle (1e-5), against the per-angle kernels (the same geometry with the
 symmetry switched off), with and without the scratch that holds the copies,
-in every memory-order pair and for every launch shape.
+in every memory-order pair and for every launch shape.  Stacks of slices
+from 32 * 2^20 pixel-angles take the orbit forward slice by slice and the
+per-angle backprojection.
 """
 
 from __future__ import annotations
@@ -60,11 +62,12 @@ def _project(ps, fwd, data, io, so, device, sym=None, work=True):
             # holds none for this precision
             ps._work_bytes[dt] = 0
             g.work, g.work_bytes = None, 0
+        tail = tuple(data.shape[2:])  # slices of a stack
         if fwd:
-            out = gg.core.empty(ps.sinogram_shape, torch.float32, so, device)
+            out = gg.core.empty(tuple(ps.sinogram_shape) + tail, torch.float32, so, device)
             gg.forwardprojection(_dev(data, io, device), ps, sino=out)
         else:
-            out = gg.core.empty(ps.img_shape, torch.float32, io, device)
+            out = gg.core.empty(tuple(ps.img_shape) + tail, torch.float32, io, device)
             gg.backprojection(_dev(data, so, device), ps, img=out)
         torch.cuda.synchronize()
         return out.double().cpu().numpy()
@@ -171,3 +174,67 @@ def test_radon_orbit_solvers(cuda_device):
     base = rel_l2(O.conjugate_gradients(f32, hps, 6), ref64)
     err = rel_l2(gg.conjugate_gradients(sino, ps, 6).double().cpu().numpy(), ref64)
     assert err <= max(1e-5, 10.0 * base), f"CG rel err {err:.3e} (float32 oracle {base:.3e})"
+
+
+@pytest.mark.parametrize("io", ["F", "C"])
+@pytest.mark.parametrize("so", ["F", "C"])
+@pytest.mark.parametrize("copies", [1, 8])
+def test_radon_orbit_stack(cuda_device, io, so, copies):
+    """A 5-slice stack of 256^2 x 512 (2^25 pixel-angles per slice, the
+    smallest that takes the orbit forward): scratch for 1 slice (one copy and
+    one forward per slice) or 8 (one copy of the 5 slices), against the
+    per-angle kernels and, for the Fortran pair, the float64 oracle.  The
+    fused reduction of CG's forward (block partials of <W q, q>, one slice's
+    after another's) covers every partial exactly once."""
+    import ctypes
+
+    import torch
+
+    import gratopy_gb300 as gg
+    from gratopy_gb300 import _lib
+
+    cfg = dict(geometry="radon", img_shape=(256, 256), angles=512, n_detectors=363)
+    ps = device_settings(cfg, cuda_device)
+    dt = np.dtype("float32")
+    assert ps.gr_geometry(dt).sym == 2
+    one = ps._work_bytes[dt]  # a single slice's: the larger, the backprojection's rows
+    assert one == 256 * (363 + 3) * 16 and one // (256 * 256 * 16) == 1
+    rng = np.random.default_rng(31 + copies + 2 * (io == "C") + 4 * (so == "C"))
+    img = rng.random(tuple(ps.img_shape) + (5,))
+    saved = dict(ps._work)
+    try:
+        ps._work_bytes[dt] = one * copies
+        ps._work = {}
+        orbit = _project(ps, True, img, io, so, cuda_device)
+        g = ps.gr_geometry(dt)
+        assert g.work_bytes == one * copies
+    finally:
+        ps._work_bytes[dt] = one
+        ps._work = saved
+    angle = _project(ps, True, img, io, so, cuda_device, sym=0)
+    assert rel_l2(orbit, angle) <= 4e-6
+    for z in range(5):  # every slice, not only the stack's norm
+        assert rel_l2(orbit[..., z], angle[..., z]) <= 4e-6, f"slice {z}"
+    if io == "F" and so == "F":
+        ref = O.forward(np.asfortranarray(img), host_settings(cfg))
+        assert rel_l2(orbit, ref) <= 1e-5
+    if io != so:
+        return
+    order = _lib.GR_ORDER_F if io == "F" else _lib.GR_ORDER_C
+    g = ps.gr_geometry(dt)
+    n = int(_lib.raw("gr_forward_partials")(ctypes.byref(g), 5))
+    assert n == 5 * int(_lib.raw("gr_forward_partials")(ctypes.byref(g), 1))
+    part = torch.full((n + 64,), float("nan"), dtype=torch.float64, device=cuda_device)
+    x = _dev(img, io, cuda_device)
+    q = gg.core.empty(tuple(ps.sinogram_shape) + (5,), torch.float32, so, cuda_device)
+    w = ps.device_tables(dt)["w"]
+    _lib.call("gr_forward_wsq", ctypes.byref(g), gg.core._ptr(q), gg.core._ptr(x),
+              gg.core._ptr(w), gg.core._ptr(part), None, 5, order,
+              gg.core._stream_ptr(cuda_device))
+    torch.cuda.synchronize()
+    got = part[:n].cpu().numpy()
+    assert np.isfinite(got).all(), "a block partial was not written"
+    assert np.isnan(part[n:].cpu().numpy()).all(), "a partial past the count was written"
+    qh = q.double().cpu().numpy()
+    want = float((qh * qh * w.double().cpu().numpy()[None, :, None]).sum())
+    assert abs(got.sum() - want) <= 1e-6 * want
