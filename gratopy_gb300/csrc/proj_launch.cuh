@@ -244,10 +244,21 @@ inline bool use_radon_orbit(const gr_geometry* g, int Nz) {
          (int64_t)(g->Ns + fast::kOrbitRowPad) * (g->Na / 2) <= INT32_MAX;
 }
 
+// From this many pixel-angles the orbit forward reads the orbit copy (one
+// 16-byte load per candidate) instead of gathering the four orbit members
+// from the image, whose turned members walk across rows (measured, us per
+// forward with / without the copy at fwd_split 8: 128^2 x 90 22.8 / 19.3,
+// 256^2 x 180 28.6 / 30.0, 512^2 x 360 73.6 / 132.7, 2048^2 x 1440 2653 /
+// 7106).
+constexpr int64_t kRadonFwdCopyMin = 4ll << 20;
+
 inline size_t radon_orbit_fwd_bytes(const gr_geometry* g, int Nz) {
-  if (!use_radon_orbit(g, Nz) || (Nz > 1 && pixel_angles(g) < kRadonOrbitStackMin)) return 0;
+  if (!use_radon_orbit(g, Nz) || pixel_angles(g) < kRadonFwdCopyMin ||
+      (Nz > 1 && pixel_angles(g) < kRadonOrbitStackMin))
+    return 0;
   return (size_t)g->Nx * (size_t)g->Ny * sizeof(float4);
 }
+
 
 inline size_t radon_orbit_bwd_bytes(const gr_geometry* g, int Nz) {
   if (!use_radon_orbit(g, Nz) || Nz != 1 || g->Nx % 2 != 0) return 0;
@@ -275,8 +286,13 @@ inline int work_slices(const gr_geometry* g, size_t per_slice, int Nz) {
 }
 
 
+// The orbit forward: single slices (without the copy, gathering the orbit
+// members: still ahead of the per-angle kernel, 512^2 x 360 133 vs 160 us),
+// and stacks of large slices with their copies (gathering, 512^2 x 360 x 16
+// ran 766 Gpixel-angle/s against the 4-slice per-angle kernel's 919).
 inline bool use_radon_orbit_fwd(const gr_geometry* g, int Nz) {
-  return work_slices(g, radon_orbit_fwd_bytes(g, Nz), Nz) > 0;
+  if (!use_radon_orbit(g, Nz)) return false;
+  return Nz == 1 || work_slices(g, radon_orbit_fwd_bytes(g, Nz), Nz) > 0;
 }
 
 inline bool use_radon_orbit_bwd(const gr_geometry* g, int Nz) {
@@ -340,15 +356,30 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
   if constexpr (std::is_same<T, float>::value) {
     if (g->kind == GR_RADON) {
       if (use_radon_orbit_fwd(g, Nz)) {
-        // half-circle orbits, slices in chunks: each pixel's four orbit pixels
-        // as one float4, then the forward over the orbits, one launch per
-        // slice (each launch's block partials follow the previous slice's)
+        // half-circle orbits, one launch per slice (each launch's block
+        // partials follow the previous slice's); four times the lanes per
+        // group: a group's work is shared by four outputs, so the orbit
+        // forward has a quarter of the groups (256^2 x 180: 16 lanes 41.6
+        // us, 8 lanes 63.4 us, 32 lanes 29.8 us)
         const fast::QuarterMaps qm = quarter_maps(g);
-        float4* img4 = static_cast<float4*>(g->work);
-        const int chunk = work_slices(g, radon_orbit_fwd_bytes(g, Nz), Nz);
-        const int64_t slice4 = (int64_t)g->Nx * g->Ny;
+        const float* ofs = static_cast<const float*>(g->ofs);
         const dim3 sgrid(grid.x, grid.y, 1);
         const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
+        int64_t sx, sy, sz;
+        img_strides<IO>(d, sx, sy, sz);
+        const int chunk = work_slices(g, radon_orbit_fwd_bytes(g, Nz), Nz);
+        if (chunk == 0) {
+          // no copy: the four orbit members gathered from the image
+          for (int64_t z = 0; z < Nz; ++z)
+            fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, false, Epi><<<sgrid, kFwdBlock, 0, st>>>(
+                img + z * sz, nullptr, ofs, radon_geo<float>(g->geo), d, qm, epi,
+                partials ? partials + z * per_slice_blocks : nullptr, skip, z);
+          return check_launch();
+        }
+        // slices in chunks: each pixel's four orbit pixels as one float4,
+        // then the forward over the copies
+        float4* img4 = static_cast<float4*>(g->work);
+        const int64_t slice4 = (int64_t)g->Nx * g->Ny;
         for (int z0 = 0; z0 < Nz; z0 += chunk) {
           const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;
           if constexpr (IO == ORDER_F) {
@@ -360,14 +391,11 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
             const dim3 pgrid((g->Nx + 255) / 256, g->Ny, zc);
             fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, z0, skip);
           }
-          // four times the lanes per group: a group's work is shared by four
-          // outputs, so the orbit forward has a quarter of the groups (256^2 x
-          // 180: 16 lanes 41.6 us, 8 lanes 63.4 us, 32 lanes 29.8 us)
           for (int c = 0; c < zc; ++c) {
             const int64_t z = z0 + c;
-            fast::radon_fwd_quarter<SO, 4 * SPLIT, Epi><<<sgrid, kFwdBlock, 0, st>>>(
-                img4 + c * slice4, static_cast<const float*>(g->ofs), radon_geo<float>(g->geo),
-                d, epi, partials ? partials + z * per_slice_blocks : nullptr, skip, z);
+            fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, true, Epi><<<sgrid, kFwdBlock, 0, st>>>(
+                img + z * sz, img4 + c * slice4, ofs, radon_geo<float>(g->geo), d, qm, epi,
+                partials ? partials + z * per_slice_blocks : nullptr, skip, z);
           }
         }
         return check_launch();

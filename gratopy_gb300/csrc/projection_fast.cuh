@@ -1482,12 +1482,16 @@ __device__ __forceinline__ int radon_orbit_half(int64_t Ns) { return (int)((Ns +
 // the image's y axis: its lanes then take adjacent image columns and walk
 // down them, so a load instruction reads adjacent pixels of the orbit copy.
 // Two candidates per trip, packed pair sums, branch-free hat weights, as in
-// fan_fwd_quarter.
-template <int SO, int SPLIT, class Epi>
-__device__ __forceinline__ double radon_fwd_quarter_tile(const float4* __restrict__ img4,
+// fan_fwd_quarter.  PIX4: the four members of a pixel's orbit come from the
+// orbit copy (one 16-byte load); otherwise from the slice `img` itself
+// through the maps (four loads).
+template <int SO, int IO, int SPLIT, bool PIX4, class Epi>
+__device__ __forceinline__ double radon_fwd_quarter_tile(const float* __restrict__ img,
+                                                         const float4* __restrict__ img4,
                                                          const float* __restrict__ ofs,
-                                                         RadonGeo<float> g, Dims d, Epi epi,
-                                                         uint3 bid, int64_t z) {
+                                                         RadonGeo<float> g, Dims d,
+                                                         QuarterMaps qm, Epi epi, uint3 bid,
+                                                         int64_t z) {
   constexpr int kOrbit = 4;
   const QuarterLayout<SPLIT> L(bid);
   const int64_t s0 = L.s0;
@@ -1517,18 +1521,48 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float4* __restric
     const float alo = (c_lo - base) * yinv, ahi = (c_hi - base) * yinv;
     int x0, x1;
     row_range(alo, bx, ahi, bx, (float)(N - 1), N, x0, x1);
-    const int stp = N;  // the orbit copy is x-fastest
+    // element steps along x and y of the pixel and of its three orbit
+    // members (the orbit copy is x-fastest; a slice has < 2^31 pixels)
+    int sx, sy, mstep_x[3] = {0, 0, 0}, mstep_y[3] = {0, 0, 0}, mbase[3] = {0, 0, 0};
+    if constexpr (PIX4) {
+      sx = 1;
+      sy = N;
+    } else {
+      int64_t sx_, sy_, sz_;
+      img_strides<IO>(d, sx_, sy_, sz_);
+      sx = (int)sx_;
+      sy = (int)sy_;
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        mstep_x[m] = qm.axx[m] * sx + qm.ayx[m] * sy;
+        mstep_y[m] = qm.axy[m] * sx + qm.ayy[m] * sy;
+        mbase[m] = qm.cx[m] * sx + qm.cy[m] * sy;
+      }
+    }
     for (int x = x0 + L.lane_group; x <= x1; x += SPLIT) {
       const float xf = (float)x;
       const int ylo = max(0, (int)ceilf(fmaf(bx, xf, alo)));
       const int yhi = min(N - 1, (int)floorf(fmaf(bx, xf, ahi)));
       float pos = fmaf(Y, (float)ylo, fmaf(X, xf, base));
-      int o0 = ylo * stp + x;
+      int o0 = ylo * sy + x * sx;
+      int om[3];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) om[m] = mbase[m] + x * mstep_x[m] + ylo * mstep_y[m];
       for (int y = ylo; y <= yhi; y += 2) {
         const bool two = y < yhi;
         const float pb = pos + Y;
-        const float4 pa4 = __ldg(img4 + o0);
-        const float4 pb4 = __ldg(img4 + (two ? o0 + stp : o0));
+        float4 pa4, pb4;
+        if constexpr (PIX4) {
+          pa4 = __ldg(img4 + o0);
+          pb4 = __ldg(img4 + (two ? o0 + sy : o0));
+        } else {
+          pa4 = make_float4(ldg(img + o0), ldg(img + om[0]), ldg(img + om[1]), ldg(img + om[2]));
+          pb4 = two ? make_float4(ldg(img + o0 + sy), ldg(img + om[0] + mstep_y[0]),
+                                  ldg(img + om[1] + mstep_y[1]), ldg(img + om[2] + mstep_y[2]))
+                    : pa4;
+#pragma unroll
+          for (int m = 0; m < 3; ++m) om[m] += 2 * mstep_y[m];
+        }
         const float mb = two ? 1.0f : 0.0f;  // a masked second candidate adds zeros
         const float2 a01 = make_float2(pa4.x, pa4.y), a23 = make_float2(pa4.z, pa4.w);
         const float2 mb2 = make_float2(mb, mb);
@@ -1542,7 +1576,7 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float4* __restric
           acc01[q] = __ffma2_rn(wb2, b01, __ffma2_rn(wa2, a01, acc01[q]));
           acc23[q] = __ffma2_rn(wb2, b23, __ffma2_rn(wa2, a23, acc23[q]));
         }
-        o0 += 2 * stp;
+        o0 += 2 * sy;
         pos = pb + Y;
       }
     }
@@ -1581,15 +1615,17 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float4* __restric
   return part;
 }
 
-// One launch per slice: img4 points at slice z's orbit copy.
-template <int SO, int SPLIT, class Epi>
+// One launch per slice: img points at slice z, img4 at its orbit copy (PIX4).
+template <int SO, int IO, int SPLIT, bool PIX4, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
-radon_fwd_quarter(const float4* __restrict__ img4, const float* __restrict__ ofs,
-                  RadonGeo<float> g, Dims d, Epi epi, double* __restrict__ partials,
-                  const int* __restrict__ skip, int64_t z) {
+radon_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4,
+                  const float* __restrict__ ofs, RadonGeo<float> g, Dims d, QuarterMaps qm,
+                  Epi epi, double* __restrict__ partials, const int* __restrict__ skip,
+                  int64_t z) {
   __shared__ double red[32];
   if (skip != nullptr && *skip) return;
-  const double part = radon_fwd_quarter_tile<SO, SPLIT, Epi>(img4, ofs, g, d, epi, blockIdx, z);
+  const double part = radon_fwd_quarter_tile<SO, IO, SPLIT, PIX4, Epi>(img, img4, ofs, g, d, qm,
+                                                                       epi, blockIdx, z);
   if (Epi::kReduce) {
     const double t = block_sum(part, red);
     if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
@@ -1680,6 +1716,7 @@ radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__
   rows4 += (int64_t)blockIdx.z * Q * nrow;
   // (P0, P3) (P2, P1) (P1, P0) (P3, P2)
   float2 A = make_float2(0.f, 0.f), B = A, C = A, D = A;
+#pragma unroll 2
   for (int k = grp; k < Q; k += G) {
     const float X = ldg(ofs + 8 * k), Y = ldg(ofs + 8 * k + 1);
     const float2 W = make_float2(ldg(ofs + 8 * k + 4), ldg(ofs + 8 * (k + Q) + 4));

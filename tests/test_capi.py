@@ -162,13 +162,28 @@ def test_host_only_entry_points(library):
     assert need == max(256 * 256 * 16, 90 * (363 + 3) * 16)
     assert work(ctypes.byref(r), 2) == 0  # stacks of slices below 32 * 2^20 pixel-angles
     r.fwd_split, r.bwd_split = 8, 8
-    no_work = fwd_parts(ctypes.byref(r), 1)
-    assert no_work == -(-363 // 32) * 180  # per-angle forward, 16 lanes per group
+    # the orbit forward with or without its copy (without, it gathers the
+    # orbit members from the image), 32 lanes per group
+    orbit_fwd = -(-182 // 8) * 45
+    assert fwd_parts(ctypes.byref(r), 1) == orbit_fwd
+    no_work_bwd = bwd_parts(ctypes.byref(r), 1, 0)  # per-angle backprojection
     r.work, r.work_bytes = ctypes.c_void_p(1 << 20), need
-    assert fwd_parts(ctypes.byref(r), 1) == -(-182 // 8) * 45  # 32 lanes per group
+    assert fwd_parts(ctypes.byref(r), 1) == orbit_fwd
     assert bwd_parts(ctypes.byref(r), 1, 0) == 4 * 128
-    r.work_bytes = 256 * 256 * 16 - 16  # too small for the forward's copy
-    assert fwd_parts(ctypes.byref(r), 1) == no_work
+    r.work_bytes = 90 * (363 + 3) * 16 - 16  # too small for the backprojection's copy
+    assert bwd_parts(ctypes.byref(r), 1, 0) == no_work_bwd
+    r.sym = 0
+    assert fwd_parts(ctypes.byref(r), 1) == -(-363 // 32) * 180  # per-angle, 16 lanes per group
+    assert bwd_parts(ctypes.byref(r), 1, 0) == no_work_bwd
+    r.sym = 2
+    # below 4 * 2^20 pixel-angles the forward gathers without a copy
+    r.Nx = r.Ny = 128
+    r.Ns, r.Na = 182, 90
+    for m, row in enumerate([(0, -1, 1, 0, 127, 0), (-1, 0, 0, -1, 127, 127),
+                             (0, 1, -1, 0, 0, 127)]):
+        for k, v in enumerate(row):
+            r.sym_map[m][k] = v
+    assert work(ctypes.byref(r), 1) == 45 * (182 + 3) * 16
     # stacks of larger slices: the orbit forward slice by slice (one slice's
     # copy per slice, up to 8 per launch pair), the per-angle backprojection
     r.Nx = r.Ny = 512

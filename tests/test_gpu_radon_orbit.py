@@ -6,10 +6,14 @@ weights over the four outputs (s, k), (s, k + Na/2), (Ns-1-s, k),
 (Ns-1-s, k + Na/2), and the backprojection shares two detector positions
 over the eight pixel-angles of a pixel orbit.  Checked against the float64
 oracle (1e-5), against the per-angle kernels (the same geometry with the
-symmetry switched off), with and without the scratch that holds the copies,
-in every memory-order pair and for every launch shape.  Stacks of slices
-from 32 * 2^20 pixel-angles take the orbit forward slice by slice and the
-per-angle backprojection.
+symmetry switched off), with the scratch that holds the copies and without
+it, in every memory-order pair and for every launch shape.  The forward of a
+single slice reads the orbit copy from 4 * 2^20 pixel-angles (the bench
+geometry here) and gathers the four orbit members from the image below that
+or without scratch (the other geometries here); both give the same sums.
+Stacks of slices from 32 * 2^20 pixel-angles take the orbit forward slice by
+slice when the scratch holds a slice's copy, and the per-angle
+backprojection.
 """
 
 from __future__ import annotations
@@ -84,7 +88,9 @@ def test_radon_orbit_parity(cuda_device, name, io, so):
     hps = host_settings(cfg)
     assert ps.quarter_maps() is not None and ps.gr_geometry(np.float32).sym == 2
     g = ps.gr_geometry(np.float32)
-    assert g.work and g.work_bytes > 0
+    # scratch for the copies; none for the odd side (no backprojection copy)
+    # below 4 * 2^20 pixel-angles (no forward copy)
+    assert bool(g.work) == (name != "odd_side") and g.work_bytes == ps._work_bytes[np.dtype("f4")]
     rng = np.random.default_rng(len(name) + 7 * (io == "C") + 13 * (so == "C"))
     img = rng.random(ps.img_shape)
     sino = rng.random(ps.sinogram_shape)
@@ -102,8 +108,12 @@ def test_radon_orbit_parity(cuda_device, name, io, so):
     # the same sums in another order as the per-angle kernels
     assert rel_l2(orbit_f, angle_f) <= 4e-6
     assert rel_l2(orbit_b, angle_b) <= 4e-6
-    # without scratch the per-angle kernels run (same results as sym 0)
-    assert rel_l2(bare_f, angle_f) <= 1e-7
+    # without scratch the orbit forward gathers the four orbit members from
+    # the image (the same sums as from the copy, bit for bit) and the
+    # per-angle backprojection runs (as with sym 0)
+    if name == "bench":
+        assert ps.gr_geometry(np.float32).work_bytes >= 256 * 256 * 16
+    assert np.array_equal(bare_f, orbit_f)
     assert rel_l2(bare_b, angle_b) <= 1e-7
 
 
@@ -178,12 +188,13 @@ def test_radon_orbit_solvers(cuda_device):
 
 @pytest.mark.parametrize("io", ["F", "C"])
 @pytest.mark.parametrize("so", ["F", "C"])
-@pytest.mark.parametrize("copies", [1, 8])
+@pytest.mark.parametrize("copies", [0, 1, 8])
 def test_radon_orbit_stack(cuda_device, io, so, copies):
     """A 5-slice stack of 256^2 x 512 (2^25 pixel-angles per slice, the
     smallest that takes the orbit forward): scratch for 1 slice (one copy and
     one forward per slice) or 8 (one copy of the 5 slices), against the
-    per-angle kernels and, for the Fortran pair, the float64 oracle.  The
+    per-angle kernels and, for the Fortran pair, the float64 oracle; without
+    scratch the stack keeps the per-angle kernels.  The
     fused reduction of CG's forward (block partials of <W q, q>, one slice's
     after another's) covers every partial exactly once."""
     import ctypes
@@ -205,13 +216,16 @@ def test_radon_orbit_stack(cuda_device, io, so, copies):
     try:
         ps._work_bytes[dt] = one * copies
         ps._work = {}
-        orbit = _project(ps, True, img, io, so, cuda_device)
-        g = ps.gr_geometry(dt)
-        assert g.work_bytes == one * copies
+        orbit = _project(ps, True, img, io, so, cuda_device, work=copies > 0)
+        if copies:
+            assert ps.gr_geometry(dt).work_bytes == one * copies
     finally:
         ps._work_bytes[dt] = one
         ps._work = saved
     angle = _project(ps, True, img, io, so, cuda_device, sym=0)
+    if copies == 0:
+        assert np.array_equal(orbit, angle)
+        return
     assert rel_l2(orbit, angle) <= 4e-6
     for z in range(5):  # every slice, not only the stack's norm
         assert rel_l2(orbit[..., z], angle[..., z]) <= 4e-6, f"slice {z}"
