@@ -58,6 +58,9 @@ class GrBatchProblem(ctypes.Structure):
         ("bwd_part", ctypes.c_void_p),
         ("a0", ctypes.c_float), ("a1", ctypes.c_float), ("a2", ctypes.c_float),
         ("a3", ctypes.c_float), ("a4", ctypes.c_float), ("cg_c", ctypes.c_double),
+        ("orbit", ctypes.c_int), ("sym", ctypes.c_int), ("fwd_tiles_y", ctypes.c_int),
+        ("obwd_tiles_x", ctypes.c_int), ("obwd_tiles_y", ctypes.c_int),
+        ("sym_map", (ctypes.c_int * 6) * 3),
     ]
 
 
@@ -102,11 +105,14 @@ SIGNATURES = {
     "gr_batch_problem_size": (_Z, []),
     "gr_batch_forward": (_I, [_P, _P, _I, _I, _I, _P]),
     "gr_batch_backward": (_I, [_P, _P, _I, _I, _I, _P]),
+    "gr_batch_forward_orbit": (_I, [_P, _P, _I, _I, _I, _I, _P]),
+    "gr_batch_backward_orbit": (_I, [_P, _P, _I, _I, _I, _I, _P]),
     "gr_batch_image_step": (_I, [_P, _P, _I, _I, _I, _P]),
     "gr_batch_sino_step": (_I, [_P, _P, _I, _I, _I, _P]),
     "gr_batch_scalars": (_I, [_P, _P, _I, _I, _I, _P]),
     "gr_forward_partials": (_Z, [_G, _I]),
     "gr_work_bytes": (_Z, [_G, _I]),
+    "gr_orbit_kinds": (_I, [_G, _I]),
     "gr_geometry_size": (_Z, []),
     "gr_backward_partials": (_Z, [_G, _I, _I]),
     "gr_weight_sinogram": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),

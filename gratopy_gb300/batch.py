@@ -5,9 +5,17 @@ Each problem is a float32 2-D sinogram with its own ``ProjectionSettings``
 Landweber, conjugate gradients or total variation -- the same iterations as
 :func:`gratopy_gb300.landweber`, :func:`gratopy_gb300.conjugate_gradients`
 and :func:`gratopy_gb300.total_variation`.  Every phase of an iteration is a
-single persistent launch over a (problem, tile) work list that covers all
-problems still running, so the GPU is filled by the batch rather than by any
-one problem.  Landweber and TV problems first run ``normest`` (batched as
+persistent launch over a (problem, tile) work list that covers all problems
+still running, so the GPU is filled by the batch rather than by any one
+problem.  Problems of at least 4 * 2^20 pixel-angles whose angle set has an
+orbit symmetry (fan beam: Na a multiple of 4 over the full circle; parallel
+beam: Na even over [0, pi); a square centred image) project over the orbits,
+as the per-call form does, gathering the orbit members (the batch keeps no
+copies): their tiles go to separate launches per geometry kind.  Smaller
+problems keep the per-angle tiles: their orbit tiles measured slower in the
+batch (the small mix of ``heterogeneous_problems``, sides 32-128: 609
+against 654 reconstructions/s), where the extra launches per iteration and
+the smaller quadrant tiles cost more than the shared geometry saves.  Landweber and TV problems first run ``normest`` (batched as
 well; one host synchronisation reads all norms), CG problems start at once.
 The iteration sequence is captured in CUDA graphs, one per range of
 iterations in which the set of running problems is constant.
@@ -27,6 +35,8 @@ from . import core
 _SOLVERS = {"landweber": _lib.GR_SOLVER_LANDWEBER, "cg": _lib.GR_SOLVER_CG,
             "tv": _lib.GR_SOLVER_TV}
 _RAYS_PER_LANE_GROUP = 4  # detector bins per lane group of the float32 forward kernel
+_ORBIT_ANGLE_GROUPS = 8  # angle groups of the batched orbit backprojection
+_ORBIT_MIN_PIXEL_ANGLES = 4 << 20  # smaller problems keep the per-angle tiles
 
 
 @dataclass
@@ -54,8 +64,9 @@ class BatchedReconstruction:
     """Run a list of :class:`Problem` s together on one GPU."""
 
     def __init__(self, problems, device=None, normest_iterations=50, seed=0, use_graph=True,
-                 graph_chunk=25, autotune=False):
+                 graph_chunk=25, autotune=False, orbit_min_pixel_angles=_ORBIT_MIN_PIXEL_ANGLES):
         self.problems = list(problems)
+        self.orbit_min_pixel_angles = orbit_min_pixel_angles
         if autotune:
             # per-geometry forward split from the autotuner; the per-call
             # projections of the same settings use it too
@@ -98,9 +109,7 @@ class BatchedReconstruction:
             d.Nx, d.Ny, d.Ns, d.Na = Nx, Ny, Ns, Na
             d.solver = _SOLVERS[pr.solver]
             d.fwd_split = pr.fwd_split
-            rays_per_block = (32 // pr.fwd_split) * 4 * _RAYS_PER_LANE_GROUP
-            d.fwd_tiles_x = -(-Ns // rays_per_block)
-            d.bwd_tiles_x, d.bwd_tiles_y = -(-Nx // 32), -(-Ny // 8)
+            self._tiles(d, ps, pr.fwd_split)
             geo = np.asarray(ps.struct["geo_dict"][np.dtype("float32")], dtype=np.float32)
             vals = ([geo[0], geo[1]] if not ps.is_fan
                     else [geo[0], geo[1], geo[2], geo[3], geo[4], geo[5], geo[10]])
@@ -116,9 +125,11 @@ class BatchedReconstruction:
                 "v4": torch.zeros(4 * Nx * Ny if pr.solver == "tv" else 4, dtype=torch.float32,
                                   device=dev),
                 "sc": torch.zeros(_lib.SC_COUNT, dtype=torch.float64, device=dev),
-                "fwd_part": torch.zeros(d.fwd_tiles_x * Na, dtype=torch.float64, device=dev),
-                "bwd_part": torch.zeros(d.bwd_tiles_x * d.bwd_tiles_y, dtype=torch.float64,
+                "fwd_part": torch.zeros(d.fwd_tiles_x * d.fwd_tiles_y, dtype=torch.float64,
                                         device=dev),
+                "bwd_part": torch.zeros(max(d.bwd_tiles_x * d.bwd_tiles_y,
+                                            d.obwd_tiles_x * d.obwd_tiles_y),
+                                        dtype=torch.float64, device=dev),
                 "tables": t,
             }
             self.buffers.append(bufs)
@@ -131,6 +142,47 @@ class BatchedReconstruction:
         self._desc_dev = torch.empty(ctypes.sizeof(self.desc), dtype=torch.uint8, device=dev)
         self._upload_desc()
 
+    def _tiles(self, d, ps, fwd_split):
+        """Tile counts of problem descriptor ``d``: the per-angle tiles, or the
+        orbit tiles where the library runs the orbit kernels for this
+        geometry (``gr_orbit_kinds``), checked against the library's own
+        block counts."""
+        Nx, Ny = ps.img_shape
+        Ns, Na = ps.sinogram_shape
+        g = _lib.GrGeometry.from_buffer_copy(ps.gr_geometry(np.float32))
+        g.work, g.work_bytes = None, 0
+        g.fwd_split, g.bwd_split = fwd_split, _ORBIT_ANGLE_GROUPS
+        d.orbit = int(_lib.raw("gr_orbit_kinds")(ctypes.byref(g), 1))
+        if Nx * Ny * Na < self.orbit_min_pixel_angles:
+            d.orbit = 0
+        d.sym = g.sym
+        for m in range(3):
+            for k in range(6):
+                d.sym_map[m][k] = g.sym_map[m][k]
+        rays_per_block = (32 // fwd_split) * 4 * _RAYS_PER_LANE_GROUP
+        d.fwd_tiles_x, d.fwd_tiles_y = -(-Ns // rays_per_block), Na
+        d.bwd_tiles_x, d.bwd_tiles_y = -(-Nx // 32), -(-Ny // 8)
+        d.obwd_tiles_x = d.obwd_tiles_y = 0
+        if d.orbit & 1:
+            # 128-thread blocks over a pair of base angles; 2 x fwd_split
+            # lanes per group of 4 bins (fan beam, every bin) or 4 x fwd_split
+            # (parallel beam, bins below ceil(Ns / 2))
+            lanes = (2 if ps.is_fan else 4) * fwd_split
+            bins = (32 // lanes) * 2 * _RAYS_PER_LANE_GROUP
+            covered = Ns if ps.is_fan else (Ns + 1) // 2
+            base = Na // 4 if ps.is_fan else Na // 2
+            d.fwd_tiles_x, d.fwd_tiles_y = -(-covered // bins), -(-base // 2)
+            want = int(_lib.raw("gr_forward_partials")(ctypes.byref(g), 1))
+            if want != d.fwd_tiles_x * d.fwd_tiles_y:
+                raise RuntimeError("orbit forward tiles disagree with the library's launch grid")
+        if d.orbit & 2:
+            # 32 x 1 quadrant tiles, 8 angle groups
+            half = Nx // 2
+            d.obwd_tiles_x, d.obwd_tiles_y = -(-half // 32), half
+            want = int(_lib.raw("gr_backward_partials")(ctypes.byref(g), 1, _lib.GR_ORDER_F))
+            if want != d.obwd_tiles_x * d.obwd_tiles_y:
+                raise RuntimeError("orbit backprojection tiles disagree with the library's grid")
+
     def _upload_desc(self):
         host = torch.frombuffer(bytearray(bytes(self.desc)), dtype=torch.uint8)
         self._desc_dev.copy_(host)
@@ -140,8 +192,11 @@ class BatchedReconstruction:
         for k in ids:
             d = self.desc[k]
             if kind == "fwd":
-                n = d.fwd_tiles_x * d.Na
+                n = d.fwd_tiles_x * d.fwd_tiles_y
             elif kind == "bwd":
+                n = (d.obwd_tiles_x * d.obwd_tiles_y if d.orbit & 2
+                     else d.bwd_tiles_x * d.bwd_tiles_y)
+            elif kind == "img":  # 32 x 8 pixel tiles of the whole image
                 n = d.bwd_tiles_x * d.bwd_tiles_y
             else:  # sinogram chunks of 256 bins
                 n = -(-(d.Ns * d.Na) // 256)
@@ -155,13 +210,33 @@ class BatchedReconstruction:
         arr = np.ascontiguousarray(arr[order])
         return torch.from_numpy(arr.reshape(-1)).to(self.device), len(arr)
 
+    def _proj_lists(self, ids, fwd):
+        """Work lists of a projection phase: (entry point, geometry kind or
+        None, items) for the per-angle tiles and for each kind's orbit
+        tiles; empty lists left out."""
+        bit = 1 if fwd else 2
+        kind = "fwd" if fwd else "bwd"
+        plain = [k for k in ids if not self.desc[k].orbit & bit]
+        out = [("gr_batch_forward" if fwd else "gr_batch_backward", None,
+                self._items(plain, kind))]
+        name = "gr_batch_forward_orbit" if fwd else "gr_batch_backward_orbit"
+        for geom in (_lib.GR_RADON, _lib.GR_FANBEAM):
+            sel = [k for k in ids if self.desc[k].orbit & bit and self.desc[k].kind == geom]
+            out.append((name, geom, self._items(sel, kind)))
+        return [e for e in out if e[2][1]]
+
     # ---------------------------------------------------------- launches
-    def _launch(self, name, lists, mode, grid):
+    def _launch(self, name, lists, mode, grid, geom=None):
         items, n = lists
         if n == 0:
             return
+        extra = () if geom is None else (geom,)
         _lib.call(name, ctypes.c_void_p(self._desc_dev.data_ptr()), ctypes.c_void_p(items.data_ptr()),
-                  n, mode, grid, core._stream_ptr(self.device))
+                  n, mode, *extra, grid, core._stream_ptr(self.device))
+
+    def _project(self, lists, mode, grid):
+        for name, geom, items in lists:
+            self._launch(name, items, mode, grid, geom)
 
     def _scalars(self, ids, mode, phase):
         t, n = ids
@@ -218,15 +293,15 @@ class BatchedReconstruction:
                     _lib.call("gr_sum_partials",
                               ctypes.c_void_p(self.buffers[k]["sc"].data_ptr() + 8 * _lib.SC_SUM),
                               core._ptr(dot), dot.numel(), st)
-                img_l, fwd_l, bwd_l = (self._items(need, "bwd"), self._items(need, "fwd"),
-                                       self._items(need, "bwd"))
+                img_l, fwd_l, bwd_l = (self._items(need, "img"), self._proj_lists(need, True),
+                                       self._proj_lists(need, False))
                 ids = self._ids(need)
                 M = _lib.GR_BATCH_NORMEST
 
                 def normest_step():
                     self._launch("gr_batch_image_step", img_l, M, self.grid_ew)
-                    self._launch("gr_batch_forward", fwd_l, M, self.grid_fwd)
-                    self._launch("gr_batch_backward", bwd_l, M, self.grid_bwd)
+                    self._project(fwd_l, M, self.grid_fwd)
+                    self._project(bwd_l, M, self.grid_bwd)
                     self._scalars(ids, M, 1)
 
                 # normest returns the sum taken at the start of its last
@@ -257,8 +332,7 @@ class BatchedReconstruction:
             self._upload_desc()
             cg = [k for k, pr in enumerate(self.problems) if pr.solver == "cg"]
             if cg:
-                self._launch("gr_batch_backward", self._items(cg, "bwd"), _lib.GR_BATCH_CG_INIT,
-                             self.grid_bwd)
+                self._project(self._proj_lists(cg, False), _lib.GR_BATCH_CG_INIT, self.grid_bwd)
                 self._scalars(self._ids(cg), _lib.GR_BATCH_CG_INIT, 1)
             # ---- main iterations, one graph per range of constant active set
             bounds = sorted({0} | {pr.iterations for pr in self.problems})
@@ -267,17 +341,17 @@ class BatchedReconstruction:
                 active = [k for k, pr in enumerate(self.problems) if pr.iterations > lo]
                 img_ids = [k for k in active if self.problems[k].solver in ("cg", "tv")]
                 cg_ids = [k for k in active if self.problems[k].solver == "cg"]
-                img_l = self._items(img_ids, "bwd")
-                fwd_l, bwd_l = self._items(active, "fwd"), self._items(active, "bwd")
+                img_l = self._items(img_ids, "img")
+                fwd_l, bwd_l = self._proj_lists(active, True), self._proj_lists(active, False)
                 sino_l = self._items(cg_ids, "sino")
                 cgi = self._ids(cg_ids)
 
                 def step(img_l=img_l, fwd_l=fwd_l, bwd_l=bwd_l, sino_l=sino_l, cgi=cgi):
                     self._launch("gr_batch_image_step", img_l, M, self.grid_ew)
-                    self._launch("gr_batch_forward", fwd_l, M, self.grid_fwd)
+                    self._project(fwd_l, M, self.grid_fwd)
                     self._scalars(cgi, M, 0)
                     self._launch("gr_batch_sino_step", sino_l, M, self.grid_ew)
-                    self._launch("gr_batch_backward", bwd_l, M, self.grid_bwd)
+                    self._project(bwd_l, M, self.grid_bwd)
                     self._scalars(cgi, M, 1)
 
                 self._iterate_chunk(step, hi - lo)
@@ -285,11 +359,13 @@ class BatchedReconstruction:
             pr.result = self.buffers[k]["img"]
         return [pr.result for pr in self.problems]
 
-    @staticmethod
-    def launches_per_iteration() -> int:
-        """Kernel launches per batched iteration (image step, forward, alpha,
-        sinogram step, backward, beta)."""
-        return 6
+    def launches_per_iteration(self) -> int:
+        """Kernel launches per batched iteration with every problem running:
+        image step, alpha, sinogram step and beta, and one forward and one
+        backprojection launch per tile family present (per-angle tiles,
+        parallel-beam orbit tiles, fan-beam orbit tiles)."""
+        ids = range(len(self.problems))
+        return 4 + len(self._proj_lists(ids, True)) + len(self._proj_lists(ids, False))
 
 
 def heterogeneous_problems(count=64, seed=0, device=None, landweber_iterations=200,

@@ -140,6 +140,50 @@ batch_forward_kernel(const gr_batch_problem* __restrict__ probs, const int2* __r
   }
 }
 
+// Forward over orbits (problems of kind KIND with orbit bit 1; items of
+// other problems are skipped): a tile covers a pair of base angles, the orbit
+// members gathered from the image, with the lanes per group of the per-call
+// orbit forwards (4 x fwd_split parallel beam, 2 x fan beam).  One kernel
+// per kind keeps each at its own register count.
+template <int KIND, int SPLIT>
+__device__ __forceinline__ double fwd_orbit_item(const gr_batch_problem& P, int tile, int mode) {
+  const uint3 bid = make_uint3(tile % P.fwd_tiles_x, tile / P.fwd_tiles_x, 0);
+  const float* in = (mode == GR_BATCH_NORMEST || P.solver == GR_SOLVER_LANDWEBER) ? P.img : P.i1;
+  const BatchFwdEpi e{&P, mode};
+  const fast::QuarterMaps qm = launch::quarter_maps_of(P.sym_map);
+  if constexpr (KIND == GR_RADON) {
+    RadonGeo<float> g;
+    g.delta_x = P.geo[0];
+    g.delta_xi = P.geo[1];
+    return fast::radon_fwd_quarter_tile<ORDER_F, ORDER_F, 4 * SPLIT, false, BatchFwdEpi>(
+        in, nullptr, P.ofs, g, dims2(P), qm, e, bid, 0);
+  } else {
+    return fast::fan_fwd_quarter_tile<ORDER_F, ORDER_F, 2 * SPLIT, false, BatchFwdEpi>(
+        in, nullptr, P.ofs, P.sdpd, fan_of(P), dims2(P), qm, e, bid, 0);
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kFwdBlock)
+batch_forward_orbit_kernel(const gr_batch_problem* __restrict__ probs,
+                           const int2* __restrict__ items, int n, int mode) {
+  __shared__ double red[32];
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const int2 item = items[it];
+    const gr_batch_problem& P = probs[item.x];
+    if (P.kind != KIND || !(P.orbit & 1)) continue;  // uniform per block
+    double part;
+    switch (P.fwd_split) {
+      case 1: part = fwd_orbit_item<KIND, 1>(P, item.y, mode); break;
+      case 2: part = fwd_orbit_item<KIND, 2>(P, item.y, mode); break;
+      case 4: part = fwd_orbit_item<KIND, 4>(P, item.y, mode); break;
+      default: part = fwd_orbit_item<KIND, 8>(P, item.y, mode); break;
+    }
+    const double t = block_sum(part, red);
+    if (threadIdx.x == 0) P.fwd_part[item.y] = t;
+  }
+}
+
 constexpr int kBatchPY = 2;  // pixels per thread of the batched backprojection
 
 __global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow / kBatchPY)
@@ -162,6 +206,40 @@ batch_backward_kernel(const gr_batch_problem* __restrict__ probs, const int2* __
     else
       part = fast::fan_bwd_fast_tile<ORDER_F, ORDER_F, 1, 1, kBatchPY, BatchBwdEpi>(
           in, P.ofs, P.sdpd, fan_of(P), dims2(P), e, bid);
+    const double t = block_sum(part, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0) P.bwd_part[item.y] = t;
+  }
+}
+
+// Backprojection over pixel orbits (problems of kind KIND with orbit bit 2;
+// items of other problems are skipped): a tile is 32 quadrant pixels, each
+// thread row one of 8 angle groups, as the per-call orbit backprojections
+// without scratch.
+constexpr int kBatchOrbitG = 8;
+
+template <int KIND>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+batch_backward_orbit_kernel(const gr_batch_problem* __restrict__ probs,
+                            const int2* __restrict__ items, int n, int mode) {
+  __shared__ double red[32];
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const int2 item = items[it];
+    const gr_batch_problem& P = probs[item.x];
+    if (P.kind != KIND || !(P.orbit & 2)) continue;  // uniform per block
+    const uint3 bid = make_uint3(item.y % P.obwd_tiles_x, item.y / P.obwd_tiles_x, 0);
+    const float* in;
+    if (mode == GR_BATCH_NORMEST) in = P.s1;
+    else if (mode == GR_BATCH_CG_INIT) in = P.s2;
+    else in = P.solver == GR_SOLVER_CG ? P.s2 : P.s1;
+    const BatchBwdEpi e{&P, mode};
+    const fast::QuarterMaps qm = launch::quarter_maps_of(P.sym_map);
+    double part;
+    if constexpr (KIND == GR_RADON)
+      part = fast::radon_bwd_orbit_tile<ORDER_F, ORDER_F, kBatchOrbitG, false, BatchBwdEpi>(
+          nullptr, in, P.ofs, dims2(P), qm, e, bid, 0);
+    else
+      part = fast::fan_bwd_orbit_tile<ORDER_F, ORDER_F, kBatchOrbitG, BatchBwdEpi>(
+          in, P.ofs, P.sdpd, fan_of(P), dims2(P), qm, e, bid, 0);
     const double t = block_sum(part, red);
     if (threadIdx.x + blockDim.x * threadIdx.y == 0) P.bwd_part[item.y] = t;
   }
@@ -228,8 +306,9 @@ batch_scalar_kernel(const gr_batch_problem* __restrict__ probs, const int* __res
                     int mode, int phase) {
   __shared__ double red[32];
   const gr_batch_problem& P = probs[ids[blockIdx.x]];
-  const int64_t n_fwd = (int64_t)P.fwd_tiles_x * P.Na;
-  const int64_t n_bwd = (int64_t)P.bwd_tiles_x * P.bwd_tiles_y;
+  const int64_t n_fwd = (int64_t)P.fwd_tiles_x * P.fwd_tiles_y;
+  const int64_t n_bwd = (P.orbit & 2) ? (int64_t)P.obwd_tiles_x * P.obwd_tiles_y
+                                      : (int64_t)P.bwd_tiles_x * P.bwd_tiles_y;
   double* sc = P.sc;
   if (phase == 0) {
     if (mode != GR_BATCH_MAIN || P.solver != GR_SOLVER_CG) return;
@@ -290,6 +369,22 @@ int gr_batch_backward(const gr_batch_problem* probs, const int* items, int n, in
                       void* stream) {
   return launch_items(batch_backward_kernel, dim3(kBwdTileFast, kBwdTileSlow / kBatchPY), probs,
                       items, n, mode, grid, stream);
+}
+
+int gr_batch_forward_orbit(const gr_batch_problem* probs, const int* items, int n, int mode,
+                           int kind, int grid, void* stream) {
+  if (kind != GR_RADON && kind != GR_FANBEAM) return GR_ERR_ARG;
+  return launch_items(kind == GR_RADON ? batch_forward_orbit_kernel<GR_RADON>
+                                       : batch_forward_orbit_kernel<GR_FANBEAM>,
+                      dim3(kFwdBlock), probs, items, n, mode, grid, stream);
+}
+
+int gr_batch_backward_orbit(const gr_batch_problem* probs, const int* items, int n, int mode,
+                            int kind, int grid, void* stream) {
+  if (kind != GR_RADON && kind != GR_FANBEAM) return GR_ERR_ARG;
+  return launch_items(kind == GR_RADON ? batch_backward_orbit_kernel<GR_RADON>
+                                       : batch_backward_orbit_kernel<GR_FANBEAM>,
+                      dim3(kBwdTileFast, kBwdTileSlow), probs, items, n, mode, grid, stream);
 }
 
 int gr_batch_image_step(const gr_batch_problem* probs, const int* items, int n, int mode,

@@ -69,6 +69,14 @@ size_t gr_work_bytes(const gr_geometry* g, int Nz) {
   return launch::orbit_work_bytes(g, Nz);
 }
 
+int gr_orbit_kinds(const gr_geometry* g, int Nz) {
+  if (g == nullptr || Nz <= 0 || launch::check_geometry(g) != GR_OK) return 0;
+  int k = 0;
+  if (launch::use_quarter(g, Nz) || launch::use_radon_orbit_fwd(g, Nz)) k |= 1;
+  if (launch::use_quarter_bwd(g, Nz) || launch::use_radon_orbit_bwd(g, Nz)) k |= 2;
+  return k;
+}
+
 size_t gr_geometry_size(void) { return sizeof(gr_geometry); }
 
 size_t gr_forward_partials(const gr_geometry* g, int Nz) {

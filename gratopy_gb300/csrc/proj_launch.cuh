@@ -170,8 +170,8 @@ inline bool use_quarter(const gr_geometry* g, int Nz) {
 // is even (the quadrant x, y < N/2 then holds one pixel of every orbit),
 // and a slice of the sinogram has fewer than 2^31 values (32-bit offsets).
 // The three maps are the powers of one quarter turn about the image centre.
-inline bool maps_cyclic(const gr_geometry* g) {
-  const int* m1 = g->sym_map[0];
+__host__ __device__ inline bool maps_cyclic_of(const int (*sym_map)[6]) {
+  const int* m1 = sym_map[0];
   if (m1[0] != 0 || m1[3] != 0 || m1[1] * m1[2] != -1) return false;
   // apply the first map after an affine map (axx, axy, ayx, ayy, cx, cy)
   auto after_m1 = [&](const int* f, int* out) {
@@ -188,9 +188,11 @@ inline bool maps_cyclic(const gr_geometry* g) {
   after_m1(m3, m4);
   const int id[6] = {1, 0, 0, 1, 0, 0};
   for (int k = 0; k < 6; ++k)
-    if (m2[k] != g->sym_map[1][k] || m3[k] != g->sym_map[2][k] || m4[k] != id[k]) return false;
+    if (m2[k] != sym_map[1][k] || m3[k] != sym_map[2][k] || m4[k] != id[k]) return false;
   return true;
 }
+
+inline bool maps_cyclic(const gr_geometry* g) { return maps_cyclic_of(g->sym_map); }
 
 inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
   if (!use_quarter(g, Nz) || g->Nx % 2 != 0) return false;
@@ -260,8 +262,16 @@ inline size_t radon_orbit_fwd_bytes(const gr_geometry* g, int Nz) {
 }
 
 
+// The orbit backprojection reads the row copy from this many pixel-angles
+// and gathers from the sinogram below (measured, us per backprojection with
+// / without the copy at 8 angle groups: 128^2 x 90 22.4 / 19.2, 256^2 x 180
+// 23.6 / 24.0, 512^2 x 360 66.6 / 79.7, 1024^2 x 720 350 / 503; the
+// per-angle kernel 21.8, 34.6, 100.6, 583).
+constexpr int64_t kRadonBwdCopyMin = 4ll << 20;
+
 inline size_t radon_orbit_bwd_bytes(const gr_geometry* g, int Nz) {
-  if (!use_radon_orbit(g, Nz) || Nz != 1 || g->Nx % 2 != 0) return 0;
+  if (!use_radon_orbit(g, Nz) || Nz != 1 || g->Nx % 2 != 0 || pixel_angles(g) < kRadonBwdCopyMin)
+    return 0;
   return (size_t)(g->Na / 2) * (size_t)(g->Ns + fast::kOrbitRowPad) * sizeof(float4);
 }
 
@@ -295,8 +305,10 @@ inline bool use_radon_orbit_fwd(const gr_geometry* g, int Nz) {
   return Nz == 1 || work_slices(g, radon_orbit_fwd_bytes(g, Nz), Nz) > 0;
 }
 
+// The orbit backprojection: single slices of even side, from the row copy
+// when the scratch holds it, else gathering from the sinogram.
 inline bool use_radon_orbit_bwd(const gr_geometry* g, int Nz) {
-  return work_slices(g, radon_orbit_bwd_bytes(g, Nz), Nz) > 0;
+  return use_radon_orbit(g, Nz) && Nz == 1 && g->Nx % 2 == 0;
 }
 
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
@@ -321,19 +333,21 @@ inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   return dim3((g->Ns + per_block - 1) / per_block, g->Na, (Nz + ZB - 1) / ZB);
 }
 
-inline fast::QuarterMaps quarter_maps(const gr_geometry* g) {
+__host__ __device__ inline fast::QuarterMaps quarter_maps_of(const int (*sym_map)[6]) {
   fast::QuarterMaps q;
   for (int m = 0; m < 3; ++m) {
-    q.axx[m] = g->sym_map[m][0];
-    q.axy[m] = g->sym_map[m][1];
-    q.ayx[m] = g->sym_map[m][2];
-    q.ayy[m] = g->sym_map[m][3];
-    q.cx[m] = g->sym_map[m][4];
-    q.cy[m] = g->sym_map[m][5];
+    q.axx[m] = sym_map[m][0];
+    q.axy[m] = sym_map[m][1];
+    q.ayx[m] = sym_map[m][2];
+    q.ayy[m] = sym_map[m][3];
+    q.cx[m] = sym_map[m][4];
+    q.cy[m] = sym_map[m][5];
   }
-  q.cyclic = maps_cyclic(g) ? 1 : 0;
+  q.cyclic = maps_cyclic_of(sym_map) ? 1 : 0;
   return q;
 }
+
+inline fast::QuarterMaps quarter_maps(const gr_geometry* g) { return quarter_maps_of(g->sym_map); }
 
 inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
   if (use_quarter_bwd(g, Nz) || use_radon_orbit_bwd(g, Nz)) {  // 32 x (8 / split) quadrant tiles
@@ -542,6 +556,11 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
       // copies, then the backprojection over the orbits (one slice per block)
       float4* rows4 = static_cast<float4*>(g->work);
       const int chunk = work_slices(g, radon_orbit_bwd_bytes(g, Nz), Nz);
+      if (chunk == 0) {
+        fast::radon_bwd_orbit<IO, SO, SPLIT, Epi><<<grid, block, 0, st>>>(
+            sino, static_cast<const float*>(g->ofs), d, quarter_maps(g), epi, partials, skip, 0);
+        return check_launch();
+      }
       const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
       for (int z0 = 0; z0 < Nz; z0 += chunk) {
         const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;

@@ -1195,21 +1195,22 @@ orbit_rows(const float* __restrict__ sino, const float* __restrict__ sdpd,
 // barrier in the angle loop).  The G thread groups of a block take
 // interleaved base angles and are added in a fixed order at the end.  This
 // form runs without scratch; fan_bwd_orbit_rows below reads the row copy.
+// The tile of block `bid` (32 x 8 threads) on slice z; returns the thread's
+// share of the block's reduction.
 template <int IO, int SO, int G, class Epi>
-__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
-fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
-              const float* __restrict__ sdpd, FanGeo<float> gg, Dims d, QuarterMaps qm, Epi epi,
-              double* __restrict__ partials, const int* __restrict__ skip, int64_t z0) {
+__device__ __forceinline__ double fan_bwd_orbit_tile(const float* __restrict__ sino,
+                                                     const float* __restrict__ ofs,
+                                                     const float* __restrict__ sdpd,
+                                                     FanGeo<float> gg, Dims d, QuarterMaps qm,
+                                                     Epi epi, uint3 bid, int64_t z) {
   constexpr int kOrbit = 4;
   constexpr int kRowsT = kBwdTileSlow / G;  // quadrant rows of the block tile
-  __shared__ double red[32];
-  if (skip != nullptr && *skip) return;
   const int lane = threadIdx.x, trow = threadIdx.y;
   const int grp = trow / kRowsT, trow_t = trow % kRowsT;
   const int half = (int)(d.Nx / 2);
   const int Q = (int)(d.Na / kOrbit);
-  const int px0 = (int)blockIdx.x * kBwdTileFast + lane;
-  const int py0 = (int)blockIdx.y * kRowsT + trow_t;
+  const int px0 = (int)bid.x * kBwdTileFast + lane;
+  const int py0 = (int)bid.y * kRowsT + trow_t;
   const bool own = px0 < half && py0 < half;
   int ox[kOrbit], oy[kOrbit];
   ox[0] = px0;
@@ -1235,7 +1236,6 @@ fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
   // slice are 32-bit, C-ordered slices interleave
   using Off = typename std::conditional<SO == ORDER_C, int64_t, int>::type;
   const Off ss = (Off)ss_, sa = (Off)sa_;
-  const int64_t z = z0 + blockIdx.z;
   sino += z * sz_;
   const int Ns = (int)d.Ns;
   float acc[kOrbit];
@@ -1309,6 +1309,18 @@ fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
     for (int k = 0; k < kOrbit; ++k)
       part += epi(ox[k], oy[k], z, img_index<IO>(ox[k], oy[k], z, d), acc[k]);
   }
+  return part;
+}
+
+template <int IO, int SO, int G, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
+              const float* __restrict__ sdpd, FanGeo<float> gg, Dims d, QuarterMaps qm, Epi epi,
+              double* __restrict__ partials, const int* __restrict__ skip, int64_t z0) {
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const double part = fan_bwd_orbit_tile<IO, SO, G, Epi>(sino, ofs, sdpd, gg, d, qm, epi,
+                                                         blockIdx, z0 + blockIdx.z);
   if (Epi::kReduce) {
     const double t = block_sum(part, red);
     if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
@@ -1668,23 +1680,25 @@ radon_orbit_rows(const float* __restrict__ sino, Dims d, float4* __restrict__ ro
 // (xi(k + Q, P) = xi(k, S P) and xi(k, -P) = Ns - 1 - xi(k, P)).  The row
 // values are interpolated as v0 + fr (v1 - v0) and weighted by the angle's
 // weight, as radon.cl:183-241 does; G thread groups take interleaved base
-// angles and are added in a fixed order.
-template <int IO, int G, class Epi>
-__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
-radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__ ofs, Dims d,
-                     QuarterMaps qm, Epi epi, double* __restrict__ partials,
-                     const int* __restrict__ skip, int64_t z0) {
+// angles and are added in a fixed order.  ROWS: the entries come from the
+// row copy `rows4` of slice z; otherwise they are gathered from slice z of
+// `sino` (zeros off the detector), the same values, so both forms give the
+// same sums bit for bit.  The tile of block `bid` (32 x 8 threads).
+template <int IO, int SO, int G, bool ROWS, class Epi>
+__device__ __forceinline__ double radon_bwd_orbit_tile(const float4* __restrict__ rows4,
+                                                       const float* __restrict__ sino,
+                                                       const float* __restrict__ ofs, Dims d,
+                                                       QuarterMaps qm, Epi epi, uint3 bid,
+                                                       int64_t z) {
   constexpr int kOrbit = 4;
   constexpr int kRowsT = kBwdTileSlow / G;
-  __shared__ double red[32];
-  if (skip != nullptr && *skip) return;
   const int lane = threadIdx.x, trow = threadIdx.y;
   const int grp = trow / kRowsT, trow_t = trow % kRowsT;
   const int N = (int)d.Nx, half = N / 2;
   const int Q = (int)(d.Na / 2);
   const int nrow = (int)d.Ns + kOrbitRowPad;
-  const int px0 = (int)blockIdx.x * kBwdTileFast + lane;
-  const int py0 = (int)blockIdx.y * kRowsT + trow_t;
+  const int px0 = (int)bid.x * kBwdTileFast + lane;
+  const int py0 = (int)bid.y * kRowsT + trow_t;
   const bool own = px0 < half && py0 < half;
   // S is the transpose of the first lookup map S^-1
   auto orbit = [&](int (&ox)[kOrbit], int (&oy)[kOrbit]) {
@@ -1712,8 +1726,27 @@ radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__
   const float2 mid2 = make_float2(mid1, mid1);
   const float hi = (float)d.Ns + 1.0f;
   const float2 neg = make_float2(-1.0f, -1.0f);
-  const int64_t z = z0 + blockIdx.z;  // slice; its copy is copy blockIdx.z
-  rows4 += (int64_t)blockIdx.z * Q * nrow;
+  int64_t ss_ = 0, sa_ = 0, sz_ = 0;
+  if constexpr (!ROWS) {
+    sino_strides<SO>(d, ss_, sa_, sz_);
+    sino += z * sz_;
+  }
+  // entry e of base angle k: (row_k[j], row_{k+Q}[j], row_k[Ns-1-j],
+  // row_{k+Q}[Ns-1-j]) with j = e - 1, zeros off the detector
+  auto entry = [&](const float4* row, int k, int e) -> float4 {
+    if constexpr (ROWS) {
+      return __ldg(row + e);
+    } else {
+      const int j = e - 1, jm = (int)d.Ns - 1 - j;
+      const bool in = (unsigned)j < (unsigned)d.Ns;
+      const int jj = in ? j : 0, jmm = in ? jm : 0;  // off the detector: bin 0, read and dropped
+      const float* rk = sino + (int64_t)k * sa_;
+      const float* rq = sino + (int64_t)(k + Q) * sa_;
+      const float4 v = make_float4(ldg(rk + jj * ss_), ldg(rq + jj * ss_), ldg(rk + jmm * ss_),
+                                   ldg(rq + jmm * ss_));
+      return in ? v : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+  };
   // (P0, P3) (P2, P1) (P1, P0) (P3, P2)
   float2 A = make_float2(0.f, 0.f), B = A, C = A, D = A;
 #pragma unroll 2
@@ -1722,14 +1755,14 @@ radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__
     const float2 W = make_float2(ldg(ofs + 8 * k + 4), ldg(ofs + 8 * (k + Q) + 4));
     const float2 u = __ffma2_rn(make_float2(X, X), pxr, __ffma2_rn(make_float2(Y, Y), pyr, mid2));
     const float uc[2] = {fminf(fmaxf(u.x, 0.0f), hi), fminf(fmaxf(u.y, 0.0f), hi)};
-    const float4* row = rows4 + k * nrow;
+    const float4* row = ROWS ? rows4 + k * nrow : nullptr;
     float2 lo[2], hi2[2];
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       const float fl = floorf(uc[e]);
       const float fr = uc[e] - fl;
       const int n = (int)fl;
-      const float4 e0 = __ldg(row + n), e1 = __ldg(row + n + 1);
+      const float4 e0 = entry(row, k, n), e1 = entry(row, k, n + 1);
       const float2 f2 = make_float2(fr, fr);
       const float2 l0 = make_float2(e0.x, e0.y), h0 = make_float2(e0.z, e0.w);
       lo[e] = __ffma2_rn(f2, __ffma2_rn(l0, neg, make_float2(e1.x, e1.y)), l0);
@@ -1764,6 +1797,37 @@ radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__
     for (int m = 0; m < kOrbit; ++m)
       part += epi(ox[m], oy[m], z, img_index<IO>(ox[m], oy[m], z, d), sum[m]);
   }
+  return part;
+}
+
+// From the row copy: slice z0 + blockIdx.z, its copy is copy blockIdx.z.
+template <int IO, int G, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__ ofs, Dims d,
+                     QuarterMaps qm, Epi epi, double* __restrict__ partials,
+                     const int* __restrict__ skip, int64_t z0) {
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const int64_t nrow = d.Ns + kOrbitRowPad;
+  const double part = radon_bwd_orbit_tile<IO, ORDER_F, G, true, Epi>(
+      rows4 + (int64_t)blockIdx.z * (d.Na / 2) * nrow, nullptr, ofs, d, qm, epi, blockIdx,
+      z0 + blockIdx.z);
+  if (Epi::kReduce) {
+    const double t = block_sum(part, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
+  }
+}
+
+// Gathering from the sinogram (no scratch): slice z0 + blockIdx.z.
+template <int IO, int SO, int G, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+radon_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs, Dims d,
+                QuarterMaps qm, Epi epi, double* __restrict__ partials,
+                const int* __restrict__ skip, int64_t z0) {
+  __shared__ double red[32];
+  if (skip != nullptr && *skip) return;
+  const double part = radon_bwd_orbit_tile<IO, SO, G, false, Epi>(nullptr, sino, ofs, d, qm, epi,
+                                                                  blockIdx, z0 + blockIdx.z);
   if (Epi::kReduce) {
     const double t = block_sum(part, red);
     if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;

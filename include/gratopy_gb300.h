@@ -96,6 +96,10 @@ GR_API const char* gr_error_string(int code);
 /* Scratch bytes the projections of g on Nz slices can use (gr_geometry.work;
  * at most 8 slices' copies); 0 when they use none. */
 GR_API size_t gr_work_bytes(const gr_geometry* g, int Nz);
+/* Which projections of g on Nz slices run over orbits (no counterpart in the
+ * reference): bit 1 the forward, bit 2 the backprojection; 0 for none or an
+ * invalid geometry.  Stacks' orbit forward needs g's scratch (gr_work_bytes). */
+GR_API int gr_orbit_kinds(const gr_geometry* g, int Nz);
 /* sizeof(gr_geometry), for bindings that mirror the struct. */
 GR_API size_t gr_geometry_size(void);
 /* Last CUDA error seen by this library on the calling thread (cudaError_t). */
@@ -281,15 +285,34 @@ typedef struct gr_batch_problem {
   double* bwd_part;            /* bwd_tiles_x * bwd_tiles_y partials */
   float a0, a1, a2, a3, a4;    /* Landweber: a0 = -w;  TV: sigma, sigma_l, mu2, tau, norming */
   double cg_c;                 /* CG: dx^2/ds */
+  /* Orbit tiles (no counterpart in the reference), as gr_orbit_kinds gives
+   * them for the problem's gr_geometry: bit 1 the forward runs over the
+   * orbits of sym_map (fwd_tiles_x bin tiles of 128-thread blocks per pair of
+   * base angles, gathering the orbit members from the image); bit 2 the
+   * backprojection does (gr_batch_backward_orbit over the quadrant's
+   * obwd_tiles_x x obwd_tiles_y tiles of 32 x 1 pixels, 8 angle groups). */
+  int orbit;
+  int sym;                     /* 4: fan-beam quarter turns, 2: parallel-beam half circle */
+  int fwd_tiles_y;             /* forward tile rows: Na, or base-angle pairs with bit 1 */
+  int obwd_tiles_x, obwd_tiles_y;
+  int sym_map[3][6];
 } gr_batch_problem;
 /* sizeof(gr_batch_problem), so bindings can check their struct layout. */
 GR_API size_t gr_batch_problem_size(void);
 /* items: 2*n ints (problem index, tile index); grid: persistent block count,
- * or <= 0 for one wave of resident blocks at the kernel's occupancy. */
+ * or <= 0 for one wave of resident blocks at the kernel's occupancy.
+ * gr_batch_forward / gr_batch_backward take the problems without orbit bit 1
+ * / bit 2; gr_batch_forward_orbit / gr_batch_backward_orbit those with it,
+ * one geometry kind (GR_RADON or GR_FANBEAM) per call (items of other
+ * problems are skipped). */
 GR_API int gr_batch_forward(const gr_batch_problem* probs, const int* items, int n, int mode,
                             int grid, void* stream);
 GR_API int gr_batch_backward(const gr_batch_problem* probs, const int* items, int n, int mode,
                              int grid, void* stream);
+GR_API int gr_batch_forward_orbit(const gr_batch_problem* probs, const int* items, int n,
+                                  int mode, int kind, int grid, void* stream);
+GR_API int gr_batch_backward_orbit(const gr_batch_problem* probs, const int* items, int n,
+                                   int mode, int kind, int grid, void* stream);
 /* image-sized elementwise step over backprojection tiles: normest scaling,
  * CG p = beta p + snew, TV dual update */
 GR_API int gr_batch_image_step(const gr_batch_problem* probs, const int* items, int n, int mode,

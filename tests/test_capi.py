@@ -118,9 +118,12 @@ def test_host_only_entry_points(library):
     assert work(ctypes.byref(q), 20) == 8 * 1024 * 1024 * 16
     sized(512, 768, 360)
     assert work(ctypes.byref(q), 3) == 0
+    assert lib.gr_orbit_kinds(ctypes.byref(q), 3) == 0  # (no scratch bound in q)
     q.dtype = 1
     assert work(ctypes.byref(q), 1) == 0
+    assert lib.gr_orbit_kinds(ctypes.byref(q), 1) == 0  # float64: per-angle kernels
     q.dtype = 0
+    assert lib.gr_orbit_kinds(ctypes.byref(q), 1) == 3
     c = 511  # valid maps, not the powers of one quarter turn: the forward's only
     assert sized(512, 768, 360, [(-1, 0, 0, -1, c, c), (0, -1, 1, 0, c, 0),
                                  (0, 1, -1, 0, 0, c)]) == 512 * 512 * 16
@@ -158,32 +161,47 @@ def test_host_only_entry_points(library):
                              (0, 1, -1, 0, 0, 255)]):
         for k, v in enumerate(row):
             r.sym_map[m][k] = v
+    kinds = lib.gr_orbit_kinds
+    assert kinds(ctypes.byref(r), 1) == 3  # forward and backprojection over orbits
+    assert kinds(ctypes.byref(r), 2) == 0  # a stack of small slices: per-angle kernels
+    assert kinds(None, 1) == 0 and kinds(ctypes.byref(r), 0) == 0
     need = work(ctypes.byref(r), 1)
     assert need == max(256 * 256 * 16, 90 * (363 + 3) * 16)
     assert work(ctypes.byref(r), 2) == 0  # stacks of slices below 32 * 2^20 pixel-angles
     r.fwd_split, r.bwd_split = 8, 8
-    # the orbit forward with or without its copy (without, it gathers the
-    # orbit members from the image), 32 lanes per group
-    orbit_fwd = -(-182 // 8) * 45
+    # the orbit kernels with or without their copies (without, they gather
+    # the orbit members from the image and the sinogram): the forward 32
+    # lanes per group, the backprojection 32 x 1 quadrant tiles
+    orbit_fwd, orbit_bwd = -(-182 // 8) * 45, 4 * 128
     assert fwd_parts(ctypes.byref(r), 1) == orbit_fwd
-    no_work_bwd = bwd_parts(ctypes.byref(r), 1, 0)  # per-angle backprojection
+    assert bwd_parts(ctypes.byref(r), 1, 0) == orbit_bwd
     r.work, r.work_bytes = ctypes.c_void_p(1 << 20), need
     assert fwd_parts(ctypes.byref(r), 1) == orbit_fwd
-    assert bwd_parts(ctypes.byref(r), 1, 0) == 4 * 128
+    assert bwd_parts(ctypes.byref(r), 1, 0) == orbit_bwd
     r.work_bytes = 90 * (363 + 3) * 16 - 16  # too small for the backprojection's copy
-    assert bwd_parts(ctypes.byref(r), 1, 0) == no_work_bwd
+    assert bwd_parts(ctypes.byref(r), 1, 0) == orbit_bwd
     r.sym = 0
     assert fwd_parts(ctypes.byref(r), 1) == -(-363 // 32) * 180  # per-angle, 16 lanes per group
-    assert bwd_parts(ctypes.byref(r), 1, 0) == no_work_bwd
+    assert bwd_parts(ctypes.byref(r), 1, 0) == 8 * 256  # per-angle 32 x 1 pixel tiles
     r.sym = 2
-    # below 4 * 2^20 pixel-angles the forward gathers without a copy
+    # below 4 * 2^20 pixel-angles both gather without copies
     r.Nx = r.Ny = 128
     r.Ns, r.Na = 182, 90
     for m, row in enumerate([(0, -1, 1, 0, 127, 0), (-1, 0, 0, -1, 127, 127),
                              (0, 1, -1, 0, 0, 127)]):
         for k, v in enumerate(row):
             r.sym_map[m][k] = v
-    assert work(ctypes.byref(r), 1) == 45 * (182 + 3) * 16
+    assert work(ctypes.byref(r), 1) == 0
+    assert kinds(ctypes.byref(r), 1) == 3
+    r.Nx = r.Ny = 127  # odd side: the forward only
+    for m, row in enumerate([(0, -1, 1, 0, 126, 0), (-1, 0, 0, -1, 126, 126),
+                             (0, 1, -1, 0, 0, 126)]):
+        for k, v in enumerate(row):
+            r.sym_map[m][k] = v
+    assert kinds(ctypes.byref(r), 1) == 1
+    r.sym = 0
+    assert kinds(ctypes.byref(r), 1) == 0
+    r.sym = 2
     # stacks of larger slices: the orbit forward slice by slice (one slice's
     # copy per slice, up to 8 per launch pair), the per-angle backprojection
     r.Nx = r.Ny = 512

@@ -59,24 +59,44 @@ def _problems(device):
     return out
 
 
+# problems of _problems whose angle sets have an orbit symmetry (square
+# centred images; fan beam Na a multiple of 4, parallel beam Na even over
+# [0, pi)): with the size floor lifted the batch runs them on orbit tiles,
+# forward and backprojection
+ORBIT_PROBLEMS = {1: 3, 2: 3, 3: 3, 5: 3}
+
+
 def test_batched_matches_per_call(cuda_device):
+    import ctypes
+
     import gratopy_gb300 as gg
+    from gratopy_gb300 import _lib
     from gratopy_gb300 import batch as gb
 
     problems = _problems(cuda_device)
-    runner = gb.BatchedReconstruction(problems, cuda_device, normest_iterations=20)
+    default = gb.BatchedReconstruction(problems, cuda_device)
+    assert not any(default.desc[k].orbit for k in range(len(problems)))  # all below 4 Mi
+    assert default.launches_per_iteration() == 6
+    runner = gb.BatchedReconstruction(problems, cuda_device, normest_iterations=20,
+                                      orbit_min_pixel_angles=0)
+    assert {k: runner.desc[k].orbit for k in range(len(problems))
+            if runner.desc[k].orbit} == ORBIT_PROBLEMS
+    assert runner.launches_per_iteration() == 4 + 3 + 3
     results = runner.run()
-    for pr, got in zip(problems, results):
+    for k, (pr, got) in enumerate(zip(problems, results)):
         ps = pr.settings
-        # the per-call form with the batched launch shapes (one thread row per
-        # angle set in the backprojection, every angle's own forward, and for
-        # Radon the batch's lanes per bin group: a per-call single Radon
-        # slice runs twice fwd_split lanes), so both add in the same order
+        # the per-call form with the batched launch shapes, so both add in the
+        # same order: per-angle problems with one thread row per angle set in
+        # the backprojection, every angle's own forward, and for Radon the
+        # batch's lanes per bin group (a per-call single Radon slice runs
+        # twice fwd_split lanes); orbit problems with 8 angle groups in the
+        # backprojection (their orbit forwards derive the lanes from
+        # fwd_split alike)
         g = ps.gr_geometry(np.float32)
-        g.bwd_split = 1
-        g.sym = 0
-        if ps.is_parallel:
-            g.fwd_split = pr.fwd_split // 2
+        orbit = int(_lib.raw("gr_orbit_kinds")(ctypes.byref(g), 1))
+        assert orbit == ORBIT_PROBLEMS.get(k, 0)
+        g.bwd_split = 8 if orbit & 2 else 1
+        g.fwd_split = pr.fwd_split // 2 if ps.is_parallel and not orbit & 1 else pr.fwd_split
         if pr.solver in ("landweber", "tv"):
             want_n = gg.normest(ps, 20, x0=pr.normest_x0)
             assert abs(pr.norm_estimate - want_n) <= 1e-12 * want_n
@@ -97,9 +117,9 @@ def test_batched_graph_and_direct_agree(cuda_device):
     from gratopy_gb300 import batch as gb
 
     a = gb.BatchedReconstruction(_problems(cuda_device), cuda_device, normest_iterations=10,
-                                 use_graph=True).run()
+                                 use_graph=True, orbit_min_pixel_angles=0).run()
     b = gb.BatchedReconstruction(_problems(cuda_device), cuda_device, normest_iterations=10,
-                                 use_graph=False).run()
+                                 use_graph=False, orbit_min_pixel_angles=0).run()
     for x, y in zip(a, b):
         assert (x == y).all()
 
@@ -142,7 +162,8 @@ def test_batched_against_fp64_oracle(cuda_device):
     from tests.helpers import HostSettings
 
     problems = _problems(cuda_device)
-    results = gb.BatchedReconstruction(problems, cuda_device, normest_iterations=20).run()
+    results = gb.BatchedReconstruction(problems, cuda_device, normest_iterations=20,
+                                       orbit_min_pixel_angles=0).run()
     for pr, got in zip(problems, results):
         ps = pr.settings
         hps = HostSettings(ps.geometry, ps.img_shape, np.asarray(ps.angles),
