@@ -37,6 +37,8 @@ class GrGeometry(ctypes.Structure):
         ("bwd_split", ctypes.c_int),
         ("sym", ctypes.c_int),
         ("sym_map", (ctypes.c_int * 6) * 3),
+        ("mirror", ctypes.c_int), ("mirror_pair", ctypes.c_int),
+        ("mirror_map", ctypes.c_int * 6),
         ("work", ctypes.c_void_p),
         ("work_bytes", ctypes.c_size_t),
     ]

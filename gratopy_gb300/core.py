@@ -337,6 +337,11 @@ class ProjectionSettings:
             for m, row in enumerate(maps):
                 for k, v in enumerate(row):
                     g.sym_map[m][k] = int(v)
+            mirror = self.mirror_map() if self.is_fan else None
+            if mirror is not None:
+                g.mirror, g.mirror_pair = 1, mirror[1]
+                for k, v in enumerate(mirror[0]):
+                    g.mirror_map[k] = int(v)
         self._geom[dtype] = g
         ga = _lib.GrGeometry.from_buffer_copy(g)
         ga.ofs = tables["ofs_adj"].data_ptr()
@@ -355,6 +360,18 @@ class ProjectionSettings:
             find = fan_quarter_maps if self.is_fan else radon_half_maps
             self._quarter = find(self.struct, self.img_shape)
         return self._quarter
+
+    def mirror_map(self):
+        """The mirror of a fan-beam geometry (see
+        :func:`gratopy_gb300.symmetry.fan_mirror_map`): ``(lookup, c0)`` with
+        angle ``c0 - b`` seeing the lookup's pixel as angle ``b`` sees the
+        pixel, the detector reversed; None when the geometry has none.
+        Computed once."""
+        if not hasattr(self, "_mirror"):
+            from .symmetry import fan_mirror_map
+
+            self._mirror = fan_mirror_map(self.struct, self.img_shape) if self.is_fan else None
+        return self._mirror
 
     def forward_scale(self, dtype) -> float:
         """Scale the forward kernels apply after the interpolation sums, in their arithmetic.

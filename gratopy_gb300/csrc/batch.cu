@@ -158,7 +158,7 @@ __device__ __forceinline__ double fwd_orbit_item(const gr_batch_problem& P, int 
     return fast::radon_fwd_quarter_tile<ORDER_F, ORDER_F, 4 * SPLIT, false, BatchFwdEpi>(
         in, nullptr, P.ofs, g, dims2(P), qm, e, bid, 0);
   } else {
-    return fast::fan_fwd_quarter_tile<ORDER_F, ORDER_F, 2 * SPLIT, false, BatchFwdEpi>(
+    return fast::fan_fwd_quarter_tile<ORDER_F, ORDER_F, 2 * SPLIT, false, false, BatchFwdEpi>(
         in, nullptr, P.ofs, P.sdpd, fan_of(P), dims2(P), qm, e, bid, 0);
   }
 }

@@ -38,6 +38,14 @@ inline int check_geometry(const gr_geometry* g) {
     for (int m = 0; m < 3; ++m)
       if (!valid_quarter_map(g->sym_map[m], g->Nx)) return GR_ERR_ARG;
   }
+  if (g->mirror != 0 && g->sym == 4) {
+    // a reflection (determinant -1) of a quarter-turn symmetric fan geometry
+    // (without the quarter-turn maps the mirror is not used)
+    const int* mm = g->mirror_map;
+    if (g->mirror_pair < 0 || g->mirror_pair >= g->Na || !valid_quarter_map(mm, g->Nx) ||
+        mm[0] * mm[3] - mm[1] * mm[2] != -1)
+      return GR_ERR_ARG;
+  }
   if (g->Na > 65535) return GR_ERR_TOO_BIG;
   return GR_OK;
 }
@@ -311,14 +319,25 @@ inline bool use_radon_orbit_bwd(const gr_geometry* g, int Nz) {
   return use_radon_orbit(g, Nz) && Nz == 1 && g->Nx % 2 == 0;
 }
 
+// The fan-beam orbit forward with the mirror: quarter-turn orbits with cyclic
+// maps, the mirror set, reading the orbit copy.
+inline bool use_fan_mirror_fwd(const gr_geometry* g, int Nz) {
+  return use_quarter(g, Nz) && g->mirror != 0 && maps_cyclic(g) &&
+         work_slices(g, quarter_fwd_bytes(g, Nz), Nz) > 0;
+}
+
 inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
   const int ZB = zblock(Nz);
   const int group = g->dtype == GR_F32 ? fast::kRayGroup : 1;  // bins per lane group
   const int per_block = (32 / split) * (kFwdBlock / 32) * group;
-  if (use_quarter(g, Nz)) {  // one slice per block, 2 * split lanes per group
+  if (use_quarter(g, Nz)) {
+    // one slice per block; 2 * split lanes per group, or 4 * split over the
+    // bins s < ceil(Ns/2) with the mirror
+    const bool mir = use_fan_mirror_fwd(g, Nz);
     const int apb = fast::kQuarterAnglesPerBlock;
-    const int qb = (32 / (2 * split)) * (kFwdBlock / 32 / apb) * group;
-    return dim3((g->Ns + qb - 1) / qb, (g->Na / 4 + apb - 1) / apb, Nz);
+    const int qb = (32 / ((mir ? 4 : 2) * split)) * (kFwdBlock / 32 / apb) * group;
+    const int bins = mir ? (g->Ns + 1) / 2 : g->Ns;
+    return dim3((bins + qb - 1) / qb, (g->Na / 4 + apb - 1) / apb, Nz);
   }
   if (use_radon_orbit_fwd(g, Nz)) {  // bins s < ceil(Ns/2), base angles k < Na/2
     const int apb = fast::kQuarterAnglesPerBlock;
@@ -335,6 +354,8 @@ inline dim3 fwd_grid(const gr_geometry* g, int Nz, int split) {
 
 __host__ __device__ inline fast::QuarterMaps quarter_maps_of(const int (*sym_map)[6]) {
   fast::QuarterMaps q;
+  q.mxx = q.mxy = q.myx = q.myy = q.mcx = q.mcy = 0;
+  q.mirror_pair = -1;
   for (int m = 0; m < 3; ++m) {
     q.axx[m] = sym_map[m][0];
     q.axy[m] = sym_map[m][1];
@@ -347,7 +368,20 @@ __host__ __device__ inline fast::QuarterMaps quarter_maps_of(const int (*sym_map
   return q;
 }
 
-inline fast::QuarterMaps quarter_maps(const gr_geometry* g) { return quarter_maps_of(g->sym_map); }
+inline fast::QuarterMaps quarter_maps(const gr_geometry* g) {
+  fast::QuarterMaps q = quarter_maps_of(g->sym_map);
+  if (g->mirror != 0) {
+    const int* mm = g->mirror_map;
+    q.mxx = mm[0];
+    q.mxy = mm[1];
+    q.myx = mm[2];
+    q.myy = mm[3];
+    q.mcx = mm[4];
+    q.mcy = mm[5];
+    q.mirror_pair = g->mirror_pair;
+  }
+  return q;
+}
 
 inline dim3 bwd_grid(const gr_geometry* g, int Nz, int io, int split) {
   if (use_quarter_bwd(g, Nz) || use_radon_orbit_bwd(g, Nz)) {  // 32 x (8 / split) quadrant tiles
@@ -441,6 +475,7 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
       int64_t sx, sy, sz;
       img_strides<IO>(d, sx, sy, sz);
       const int chunk = work_slices(g, quarter_fwd_bytes(g, Nz), Nz);
+      const bool mirror = use_fan_mirror_fwd(g, Nz);
       if (chunk > 0) {
         // slices in chunks: orbit-pixel copies, then the forward on them
         float4* img4 = static_cast<float4*>(g->work);
@@ -458,14 +493,20 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
           }
           for (int k = 0; k < zc; ++k) {
             const int64_t z = z0 + k;
-            fast::fan_fwd_quarter<SO, IO, kQSplit, true, Epi><<<sgrid, kFwdBlock, 0, st>>>(
-                img + z * sz, img4 + k * slice4, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi,
-                partials ? partials + z * per_slice_blocks : nullptr, skip, z);
+            double* pz = partials ? partials + z * per_slice_blocks : nullptr;
+            if (mirror)  // half the bins: twice the lanes per group
+              fast::fan_fwd_quarter<SO, IO, 2 * kQSplit, true, true, Epi>
+                  <<<sgrid, kFwdBlock, 0, st>>>(img + z * sz, img4 + k * slice4, ofs, sdpd,
+                                                fan_geo<float>(g->geo), d, qm, epi, pz, skip, z);
+            else
+              fast::fan_fwd_quarter<SO, IO, kQSplit, true, false, Epi>
+                  <<<sgrid, kFwdBlock, 0, st>>>(img + z * sz, img4 + k * slice4, ofs, sdpd,
+                                                fan_geo<float>(g->geo), d, qm, epi, pz, skip, z);
           }
         }
       } else {
         for (int64_t z = 0; z < Nz; ++z)
-          fast::fan_fwd_quarter<SO, IO, kQSplit, false, Epi><<<sgrid, kFwdBlock, 0, st>>>(
+          fast::fan_fwd_quarter<SO, IO, kQSplit, false, false, Epi><<<sgrid, kFwdBlock, 0, st>>>(
               img + z * sz, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi,
               partials ? partials + z * per_slice_blocks : nullptr, skip, z);
       }

@@ -830,11 +830,25 @@ struct QuarterMaps {
   // relation holds from every angle of an orbit, not only from the base
   // angles in [0, Na/4)
   int cyclic;
+  // fan-beam mirror (mirror_pair >= 0): angle (mirror_pair - b) mod Na sees
+  // pixel M P as angle b sees P with the detector reversed; M is the lookup
+  // (mxx, mxy, myx, myy, mcx, mcy) in the format of the maps above
+  int mxx, mxy, myx, myy, mcx, mcy;
+  int mirror_pair;
 };
 
 // img (and img4) point at slice z; offsets within a slice are 32-bit except
 // for C-ordered images, whose slices interleave.
-template <int SO, int IO, int SPLIT, bool PIX4, class Epi>
+//
+// MIRROR (with the orbit copy and cyclic maps): the geometry also has the
+// mirror M of qm (angle c0 - b sees M P as angle b sees P, the detector
+// reversed).  A reflection turns a quarter turn into its inverse, M L_m =
+// L_{-m} M, so the mirrored members img(M L_m P) are the orbit copy's entry
+// at M P in the order (0, 3, 2, 1): one more 16-byte load per candidate
+// gives the weights of bins s0 .. s0 + 3 four more outputs, at the mirrored
+// bins Ns - 1 - s of the angles c0 - (a + m Q).  The groups then walk only
+// the bins s < ceil(Ns/2) (the middle bin of an odd detector written once).
+template <int SO, int IO, int SPLIT, bool PIX4, bool MIRROR, class Epi>
 __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__ img,
                                                        const float4* __restrict__ img4,
                                                        const float* __restrict__ ofs,
@@ -842,17 +856,23 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
                                                        FanGeo<float> g, Dims d, QuarterMaps qm,
                                                        Epi epi, uint3 bid, int64_t z) {
   constexpr int kOrbit = 4;
+  static_assert(!MIRROR || PIX4, "the mirrored members come from the orbit copy");
   using Off = typename std::conditional<IO == ORDER_C && !PIX4, int64_t, int>::type;
   const QuarterLayout<SPLIT> L(bid);
   const int64_t s0 = L.s0;
   const int64_t a = L.a;                // base angle in [0, Na/4)
   const int64_t quarter = d.Na / kOrbit;
-  const bool active = s0 < d.Ns && a < quarter;
+  const int64_t Hs = MIRROR ? (d.Ns + 1) / 2 : d.Ns;  // bins the groups walk
+  const bool active = s0 < Hs && a < quarter;
   // bin q's sums for the orbit angles (0, 1) and (2, 3): one register pair
-  // each, updated by packed float32 multiply-adds (two lanes per instruction)
+  // each, updated by packed float32 multiply-adds (two lanes per instruction);
+  // with MIRROR the same for the entry at M P (mirror components 0 .. 3)
   float2 acc01[kRayGroup], acc23[kRayGroup];
+  float2 macc01[MIRROR ? kRayGroup : 1], macc23[MIRROR ? kRayGroup : 1];
 #pragma unroll
   for (int q = 0; q < kRayGroup; ++q) acc01[q] = acc23[q] = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int q = 0; q < (MIRROR ? kRayGroup : 1); ++q) macc01[q] = macc23[q] = make_float2(0.0f, 0.0f);
   const float R = g.R;
   int shift = 0;  // accumulator m belongs to row a + ((m + shift) mod 4) Na/4
   if (active) {
@@ -909,6 +929,9 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
       mstep_y[m] = (Off)(qm.axy[m] * sx + qm.ayy[m] * sy);
       mbase[m] = (Off)(qm.cx[m] * sx + qm.cy[m] * sy);
     }
+    // and of the mirrored pixel M P in the orbit copy
+    Off Mstep_x = (Off)(qm.mxx * sx + qm.myx * sy), Mstep_y = (Off)(qm.mxy * sx + qm.myy * sy);
+    const Off Mbase = (Off)(qm.mcx * sx + qm.mcy * sy);
     int64_t step_x = sx, step_y = sy;
     const bool steep = fabsf(dpx) < fabsf(dpy) && fabsf(dmx) < fabsf(dmy);
     const bool swap = !steep && dpx * dmx > 0.0f;
@@ -930,6 +953,9 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
         mstep_x[m] = mstep_y[m];
         mstep_y[m] = t2;
       }
+      const Off t3 = Mstep_x;
+      Mstep_x = Mstep_y;
+      Mstep_y = t3;
     }
     dpx /= dpy;
     dmx /= dmy;
@@ -954,6 +980,7 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
       float ss = fmaf(dx, xlf, fmaf(dy, yf, s_c));
       const Off stp = (Off)step_x;
       Off o0 = (Off)(y * step_y + xlo * step_x);
+      Off oM = MIRROR ? (Off)(Mbase + y * Mstep_y + xlo * Mstep_x) : 0;
       Off om[kOrbit - 1];
       if constexpr (!PIX4) {
 #pragma unroll
@@ -978,6 +1005,16 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
           const float2 a23 = __fmul2_rn(make_float2(pa.z, pa.w), ra2);
           const float2 b01 = __fmul2_rn(make_float2(pb.x, pb.y), rb2);
           const float2 b23 = __fmul2_rn(make_float2(pb.z, pb.w), rb2);
+          float2 ma01, ma23, mb01, mb23;
+          if constexpr (MIRROR) {
+            const float4 qa = __ldg(img4 + oM);
+            const float4 qb = __ldg(img4 + (two ? oM + Mstep_x : oM));
+            ma01 = __fmul2_rn(make_float2(qa.x, qa.y), ra2);
+            ma23 = __fmul2_rn(make_float2(qa.z, qa.w), ra2);
+            mb01 = __fmul2_rn(make_float2(qb.x, qb.y), rb2);
+            mb23 = __fmul2_rn(make_float2(qb.z, qb.w), rb2);
+            oM += 2 * Mstep_x;
+          }
 #pragma unroll
           for (int q = 0; q < kRayGroup; ++q) {
             const float wa = fmaxf(0.0f, 1.0f - fabsf((float)q - ua));
@@ -985,6 +1022,10 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
             const float2 wa2 = make_float2(wa, wa), wb2 = make_float2(wb, wb);
             acc01[q] = __ffma2_rn(wb2, b01, __ffma2_rn(wa2, a01, acc01[q]));
             acc23[q] = __ffma2_rn(wb2, b23, __ffma2_rn(wa2, a23, acc23[q]));
+            if constexpr (MIRROR) {
+              macc01[q] = __ffma2_rn(wb2, mb01, __ffma2_rn(wa2, ma01, macc01[q]));
+              macc23[q] = __ffma2_rn(wb2, mb23, __ffma2_rn(wa2, ma23, macc23[q]));
+            }
           }
           o0 += 2 * stp;
           t = tb + ddx;
@@ -1015,29 +1056,53 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
       }
     }
   }
-  float acc[kOrbit][kRayGroup];
+  constexpr int kOut = MIRROR ? 2 * kOrbit : kOrbit;
+  float acc[kOut][kRayGroup];
 #pragma unroll
   for (int q = 0; q < kRayGroup; ++q) {
     acc[0][q] = acc01[q].x;
     acc[1][q] = acc01[q].y;
     acc[2][q] = acc23[q].x;
     acc[3][q] = acc23[q].y;
+    if constexpr (MIRROR) {
+      acc[4][q] = macc01[q].x;
+      acc[5][q] = macc01[q].y;
+      acc[6][q] = macc23[q].x;
+      acc[7][q] = macc23[q].y;
+    }
   }
   if (SPLIT > 1) {
 #pragma unroll
-    for (int m = 0; m < kOrbit; ++m) warp_reduce_rows<SPLIT>(acc[m]);
+    for (int m = 0; m < kOut; ++m) warp_reduce_rows<SPLIT>(acc[m]);
   }
   double part = 0.0;
   if (active && L.lane_group == 0) {
+    const int64_t mirror_max = d.Ns - 1 - Hs;  // mirrored outputs for s <= this
 #pragma unroll
     for (int q = 0; q < kRayGroup; ++q) {
       const int64_t s = s0 + q;
-      if (s < d.Ns) {
+      if (s < Hs) {
         const float sc = sdpd[s] / g.delta_xi * g.delta_x / R;
 #pragma unroll
         for (int m = 0; m < kOrbit; ++m) {
           const int64_t am = a + ((m + shift) & (kOrbit - 1)) * quarter;
           part += epi(s, am, z, sino_index<SO>(s, am, z, d), acc[m][q] * sc);
+        }
+        if constexpr (MIRROR) {
+          if (s <= mirror_max) {
+            // component k of the entry at M P is member m = -k mod 4: the
+            // output (Ns - 1 - s, c0 - (a + ((m + shift) mod 4) Q))
+            const int64_t sm = d.Ns - 1 - s;
+            const float scm = sdpd[sm] / g.delta_xi * g.delta_x / R;
+#pragma unroll
+            for (int k = 0; k < kOrbit; ++k) {
+              const int m = (kOrbit - k) & (kOrbit - 1);
+              const int64_t am = a + ((m + shift) & (kOrbit - 1)) * quarter;
+              int64_t bm = qm.mirror_pair - am;
+              if (bm < 0) bm += d.Na;
+              part += epi(sm, bm, z, sino_index<SO>(sm, bm, z, d), acc[kOrbit + k][q] * scm);
+            }
+          }
         }
       }
     }
@@ -1834,7 +1899,9 @@ radon_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs, D
   }
 }
 
-template <int SO, int IO, int SPLIT, bool PIX4, class Epi>
+// (The mirrored kernel at 94 registers; capped at 80 for 6 blocks per SM it
+// spilled and ran 512^2 x 360 in 99.4 instead of 77.0 us.)
+template <int SO, int IO, int SPLIT, bool PIX4, bool MIRROR, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
 fan_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4,
                 const float* __restrict__ ofs,
@@ -1844,7 +1911,7 @@ fan_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4,
   // computed here instead of taken from the parameters measured 8% slower)
   __shared__ double red[32];
   if (skip != nullptr && *skip) return;
-  const double part = fan_fwd_quarter_tile<SO, IO, SPLIT, PIX4, Epi>(
+  const double part = fan_fwd_quarter_tile<SO, IO, SPLIT, PIX4, MIRROR, Epi>(
       img, img4, ofs, sdpd, g, d, qm, epi, blockIdx, z);
   if (Epi::kReduce) {
     double t = block_sum(part, red);

@@ -85,6 +85,70 @@ def fan_quarter_maps(struct, img_shape, atol_bins: float = 1e-6, rtol_t: float =
     return maps
 
 
+def fan_mirror_map(struct, img_shape, atol_bins: float = 1e-6, rtol_t: float = 1e-9):
+    """Mirror symmetry of a fan-beam geometry, or None.
+
+    With a square image centred on the rotation axis and a detector centred
+    on the central ray, a reflection M of the grid through the rotation axis
+    maps the view of angle b to the view of angle c0 - b with the detector
+    reversed: u(c0 - b, M P) = Ns - 1 - u(b, P) with the same distance
+    weight, for every angle b (angles equispaced over the full circle pair
+    up this way about the mirror axis).  Then
+
+        sino[Ns-1-s, c0 - b] = sum_P img(M P) K(b, P; s),
+
+    so a forward projection that has the weights K of angle b can fill the
+    mirrored bin of angle c0 - b as well.  Returns ``((Axx, Axy, Ayx, Ayy,
+    Cx, Cy), c0)``, the lookup M in the format of :func:`fan_quarter_maps`
+    and the angle index c0 (the pairing is b <-> (c0 - b) mod Na), checked
+    in float64 on sample pixels for every angle; None when no reflection
+    and pairing pass.
+    """
+    Nx, Ny = (int(v) for v in img_shape)
+    ofs = np.asarray(struct["ofs_dict"][np.dtype("float64")], dtype=np.float64)
+    geo = np.asarray(struct["geo_dict"][np.dtype("float64")], dtype=np.float64)
+    Na = ofs.shape[1]
+    if Nx != Ny or Na < 2:
+        return None
+    c = (Nx - 1) * 0.5
+    if geo[3] != c or geo[4] != c:
+        return None
+    R, RE, dxi, mid_det = geo[0], geo[1], geo[2], geo[5]
+    Ns = int(round(geo[8]))
+    px, py = _sample_pixels(Nx)
+    px, py = px - c, py - c
+
+    def u_t(a, X, Y):
+        XD, YD, Qx, Qy, Dx0, Dy0 = (ofs[k, a][:, None] for k in range(6))
+        t = ((Dx0 - Qx) * X + (Dy0 - Qy) * Y) / (R * R) + RE / R
+        ss = (XD * X + YD * Y) / (dxi * dxi)
+        return ss / t + mid_det, t
+
+    total = 2.0 * mid_det  # u + u' = Ns - 1 when the detector is centred
+    if abs(total - (Ns - 1)) > atol_bins:
+        return None
+    allb = np.arange(Na)
+    u_b, t_b = u_t(allb, px[None, :], py[None, :])
+    for S in _MAPS[4:8]:  # the four reflections
+        X = S[0] * px + S[1] * py
+        Y = S[2] * px + S[3] * py
+        # the angle paired with angle 0, then every angle
+        u_m, t_m = u_t(allb, X[None, :], Y[None, :])
+        cand = np.nonzero(np.all(np.abs(u_m + u_b[0][None, :] - total) <= atol_bins, axis=1)
+                          & np.all(np.abs(t_m - t_b[0][None, :])
+                                   <= rtol_t * np.abs(t_b[0][None, :]), axis=1))[0]
+        for c0 in cand:
+            pair = (int(c0) - allb) % Na
+            if (np.all(np.abs(u_m[pair] + u_b - total) <= atol_bins)
+                    and np.all(np.abs(t_m[pair] - t_b) <= rtol_t * np.abs(t_b))):
+                # a reflection is its own inverse: the lookup is M itself
+                Axx, Axy, Ayx, Ayy = S
+                Cx = int(round(c * (1 - Axx - Axy)))
+                Cy = int(round(c * (1 - Ayx - Ayy)))
+                return (Axx, Axy, Ayx, Ayy, Cx, Cy), int(c0)
+    return None
+
+
 def radon_half_maps(struct, img_shape, atol_bins: float = 1e-6):
     """Index maps of the quarter-turn-and-mirror orbit of a parallel-beam
     geometry, or None.

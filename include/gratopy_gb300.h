@@ -79,6 +79,18 @@ typedef struct gr_geometry {
    * the Python layer after checking the geometry. */
   int sym;
   int sym_map[3][6];
+  /* Mirror symmetry of a quarter-turn symmetric fan-beam geometry (sym = 4;
+   * no counterpart in the reference): nonzero when angle (mirror_pair - b)
+   * mod Na sees pixel mirror_map(P) as angle b sees P, with the detector
+   * reversed (bin s <-> Ns - 1 - s), for every angle b.  mirror_map is a
+   * reflection through the image centre in the sym_map format.  The float32
+   * forward projection that reads the orbit copy then walks only the bins
+   * s < ceil(Ns/2) and fills their mirrored bins from the same weights.
+   * Ignored unless sym = 4.  Set by the Python layer after checking the
+   * geometry; 0 in a zeroed descriptor. */
+  int mirror;
+  int mirror_pair;
+  int mirror_map[6];
   /* Device scratch (no counterpart in the reference) that a call may use
    * while it runs, stream-ordered, 16-byte aligned: the quarter-turn orbit
    * kernels keep interleaved copies of their input there (the forward: the

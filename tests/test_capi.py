@@ -140,6 +140,32 @@ def test_host_only_entry_points(library):
         q.fwd_split, q.bwd_split = fs, bs
         assert fwd_parts(ctypes.byref(q), 1) == want_f
         assert bwd_parts(ctypes.byref(q), 1, 0) == want_b
+    # the fan-beam mirror: a reflection with an angle pairing, validated
+    # with the geometry (gr_work_bytes is 0 for an invalid descriptor); the
+    # mirrored forward walks half the bins with twice the lanes, so its
+    # block count equals the quarter-turn forward's
+    sized(512, 768, 360)
+    q.fwd_split = 8
+    plain_need, plain_parts = work(ctypes.byref(q), 1), fwd_parts(ctypes.byref(q), 1)
+    q.mirror, q.mirror_pair = 1, 180
+    for k, v in enumerate((-1, 0, 0, 1, 511, 0)):
+        q.mirror_map[k] = v
+    assert work(ctypes.byref(q), 1) == plain_need
+    q.work, q.work_bytes = ctypes.c_void_p(1 << 20), plain_need
+    assert fwd_parts(ctypes.byref(q), 1) == plain_parts == 48 * 90 // 2
+    q.mirror_pair = 360  # out of range
+    assert work(ctypes.byref(q), 1) == 0
+    q.mirror_pair = 180
+    q.mirror_map[0], q.mirror_map[3] = -1, -1  # a half turn, not a reflection
+    assert work(ctypes.byref(q), 1) == 0
+    q.mirror_map[3] = 1
+    q.mirror_pair = -1  # no pairing
+    assert work(ctypes.byref(q), 1) == 0
+    q.sym, q.mirror_pair = 0, 360  # without the quarter-turn maps the mirror is ignored
+    assert lib.gr_orbit_kinds(ctypes.byref(q), 1) == 0
+    q.sym = 4
+    q.mirror = 0
+    q.work, q.work_bytes = None, 0
     sized(1024, 1536, 720)  # a stack whose slices take the orbit kernels
     q.fwd_split, q.bwd_split = 8, 8
     assert fwd_parts(ctypes.byref(q), 3) == 48 * 180 * 3

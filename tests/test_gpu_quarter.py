@@ -93,8 +93,9 @@ def test_quarter_backprojection(cuda_device, name, order, split):
     assert rel_l2(shared, direct) < 4e-6
 
 
-def _raw(ps, fwd, data_np, work, work_bytes, cuda_device):
-    """One projection through gr_forward / gr_backward with the given scratch."""
+def _raw(ps, fwd, data_np, work, work_bytes, cuda_device, mirror=True):
+    """One projection through gr_forward / gr_backward with the given scratch
+    (and the geometry's mirror switched off with ``mirror=False``)."""
     import ctypes
 
     import torch
@@ -104,6 +105,8 @@ def _raw(ps, fwd, data_np, work, work_bytes, cuda_device):
 
     g = _lib.GrGeometry.from_buffer_copy(ps.gr_geometry(np.float32))
     g.work, g.work_bytes = work, work_bytes
+    if not mirror:
+        g.mirror = 0
     in_shape, out_shape = ((ps.img_shape, ps.sinogram_shape) if fwd
                            else (ps.sinogram_shape, ps.img_shape))
     x = gg.core.empty(in_shape, torch.float32, "F", cuda_device)
@@ -135,7 +138,10 @@ def test_small_problems_bind_no_scratch(cuda_device):
 @pytest.mark.parametrize("fwd", [True, False])
 def test_orbit_scratch_and_direct_gather_agree(cuda_device, name, fwd):
     """With the interleaved scratch copy, without scratch, and with scratch
-    one float4 too small (the kernels then read their input directly)."""
+    one float4 too small (the kernels then read their input directly).  The
+    copy and the direct gathers sum in the same order within 1e-6 with the
+    mirror switched off; the forward from the copy with the mirror (the bins
+    beyond the middle from the mirrored weights) within 4e-6."""
     import ctypes
 
     from gratopy_gb300 import _lib
@@ -162,10 +168,12 @@ def test_orbit_scratch_and_direct_gather_agree(cuda_device, name, fwd):
         data = rng.random(ps.sinogram_shape)
         ref = O.backward(np.asfortranarray(data), hps)
         own = bwd_need
-    with_copy = _raw(ps, fwd, data, g.work, need, cuda_device)
+    with_copy = _raw(ps, fwd, data, g.work, need, cuda_device, mirror=False)
     direct = _raw(ps, fwd, data, None, 0, cuda_device)
     assert rel_l2(with_copy, ref) < 1e-5 and rel_l2(direct, ref) < 1e-5
     assert rel_l2(with_copy, direct) < 1e-6
+    mirrored = _raw(ps, fwd, data, g.work, need, cuda_device)
+    assert rel_l2(mirrored, ref) < 1e-5 and rel_l2(mirrored, direct) < 4e-6
     if own:
         small = _raw(ps, fwd, data, g.work, own - 16, cuda_device)
         assert (small == direct).all()
@@ -177,7 +185,7 @@ STACK_CFG = dict(geometry="fanbeam", img_shape=(768, 768), angles=480, n_detecto
                  detector_width=400.0, R=400.0, RE=200.0)
 
 
-def _stack_call(ps, fwd, x, nz, order, work, work_bytes, cuda_device, sym=4):
+def _stack_call(ps, fwd, x, nz, order, work, work_bytes, cuda_device, sym=4, mirror=True):
     import ctypes
 
     import torch
@@ -187,6 +195,8 @@ def _stack_call(ps, fwd, x, nz, order, work, work_bytes, cuda_device, sym=4):
 
     g = _lib.GrGeometry.from_buffer_copy(ps.gr_geometry(np.float32))
     g.sym, g.work, g.work_bytes = sym, work, work_bytes
+    if not mirror:
+        g.mirror = 0
     shape = (ps.sinogram_shape if fwd else ps.img_shape) + (nz,)
     out = gg.core.empty(shape, torch.float32, order, cuda_device)
     of = core._oflag(order)
@@ -223,10 +233,15 @@ def test_orbit_kernels_on_stacks(cuda_device, order, fwd):
             for k in (1, 2, 3)}
     direct = _stack_call(ps, fwd, x, nz, order, None, 0, cuda_device)
     per_angle = _stack_call(ps, fwd, x, nz, order, None, 0, cuda_device, sym=0)
+    unmirrored = _stack_call(ps, fwd, x, nz, order, buf.data_ptr(), per_slice, cuda_device,
+                             mirror=False)
     assert torch.equal(runs[1], runs[2]) and torch.equal(runs[1], runs[3])
     d = direct.double().cpu().numpy()
     r = runs[1].double().cpu().numpy()
-    assert rel_l2(r, d) < 1e-6
+    # the copy against the direct gathers with the mirror off (the same
+    # order of sums), and with the mirror (another order for half the bins)
+    assert rel_l2(unmirrored.double().cpu().numpy(), d) < 1e-6
+    assert rel_l2(r, d) < (4e-6 if fwd else 1e-6)
     assert rel_l2(r, per_angle.double().cpu().numpy()) < 4e-6
     for k in (0, nz - 1):
         sl = np.asfortranarray(data[:, :, k])

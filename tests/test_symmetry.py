@@ -101,3 +101,54 @@ def test_radon_asymmetric_geometries_are_rejected(name):
 
     ps = host_settings(dict(RADON_BASE, **RADON_ASYMMETRIC[name]))
     assert radon_half_maps(ps.struct, ps.img_shape) is None
+
+
+# fan beam: the mirror (reflection through the axis, detector reversed)
+MIRROR_SYMMETRIC = {
+    "plain": {},
+    "reversed_detector": dict(reverse_detector=True),
+    "odd_side": dict(img_shape=(37, 37), angles=20),
+    "odd_detectors": dict(n_detectors=63),
+    "half_circle": dict(angles=[(36, 0.0, np.pi)]),
+    "bench": dict(img_shape=(64, 64), angles=360, n_detectors=96, detector_width=400.0,
+                  R=400.0, RE=200.0),
+}
+MIRROR_ASYMMETRIC = {
+    "shifted_detector": dict(detector_shift=3.0),
+    "shifted_image": dict(midpoint_shift=(1.0, 0.0)),
+    "not_square": dict(img_shape=(40, 36)),
+    "uneven_angles": dict(angles=[0.0, 0.3, 1.1, 2.0, 4.0]),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MIRROR_SYMMETRIC))
+def test_fan_mirror_maps_reversed_views(name):
+    """For the mirror (M, c0): the oracle's projection of the image looked up
+    through M, at angle b and bin s, equals the original image's projection
+    at angle (c0 - b) mod Na and bin Ns - 1 - s (float64, 1e-12)."""
+    from gratopy_gb300.symmetry import fan_mirror_map
+
+    ps = host_settings(dict(BASE, **MIRROR_SYMMETRIC[name]))
+    found = fan_mirror_map(ps.struct, ps.img_shape)
+    assert found is not None
+    (axx, axy, ayx, ayy, cx, cy), c0 = found
+    assert axx * ayy - axy * ayx == -1  # a reflection
+    N = ps.img_shape[0]
+    Ns, Na = ps.sinogram_shape
+    img = np.asfortranarray(np.random.default_rng(2).random((N, N)))
+    sino = O.forward(img, ps)
+    x, y = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
+    mx, my = cx + axx * x + axy * y, cy + ayx * x + ayy * y
+    assert mx.min() == 0 and mx.max() == N - 1 and my.min() == 0 and my.max() == N - 1
+    mirrored = O.forward(np.asfortranarray(img[mx, my]), ps)
+    b = np.arange(Na)
+    err = np.abs(mirrored[:, b] - sino[::-1, (c0 - b) % Na]).max()
+    assert err <= 1e-12 * np.abs(sino).max()
+
+
+@pytest.mark.parametrize("name", sorted(MIRROR_ASYMMETRIC))
+def test_fan_mirror_rejected(name):
+    from gratopy_gb300.symmetry import fan_mirror_map
+
+    ps = host_settings(dict(BASE, **MIRROR_ASYMMETRIC[name]))
+    assert fan_mirror_map(ps.struct, ps.img_shape) is None
