@@ -212,10 +212,11 @@ inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
 // pixel) and the backprojection's interleaved rows (one float4 per base
 // angle and bin); one call uses one of them, so the larger one is needed.
 // Below these sizes (pixel-angles per projection) the extra launch costs more
-// than the copy saves (measured: the forward's copy loses at 256^2 x 360 and
-// wins at 512^2 x 360, the backprojection's loses at 128^2 x 360 and wins at
-// 256^2 x 360).
-constexpr int64_t kQuarterFwdCopyMin = 48ll << 20;
+// than the copy saves (measured, fan beam with 360 angles, us per forward at
+// the best split, copy with the mirror against direct gathers: 128^2 26.6 /
+// 24.7, 192^2 31.9 / 31.4, 256^2 38.6 / 42.5, 384^2 54.9 / 77.0; the
+// backprojection's copy loses at 128^2 and wins at 256^2).
+constexpr int64_t kQuarterFwdCopyMin = 16ll << 20;
 constexpr int64_t kQuarterBwdCopyMin = 12ll << 20;
 // slices copied per launch pair at most (a stack runs in chunks of as many
 // slices as the scratch holds)

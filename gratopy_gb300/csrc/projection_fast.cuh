@@ -1411,7 +1411,11 @@ fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
 //    added at the end.
 // Every value is rounded as in fan_bwd_orbit: t = ddx x + (ddy y + tz),
 // s likewise, xi = s / t + midpoint, weights (1 - fr) / t and fr / t, the
-// angle weight / R by division.
+// angle weight / R by division.  (Owning the eight-pixel orbits of the
+// geometry's mirror as well -- the mirrored rows in a second plane of the
+// copy, the quadrant's pixels x <= y -- measured slower: 512^2 x 360 77.2
+// against 68.2 us, 2048^2 x 1440 3001 against 2620 us; the same L1 bytes per
+// pixel-angle from half the threads, each with twice the footprint.)
 template <int IO, int G, class Epi>
 __global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
 fan_bwd_orbit_rows(const float4* __restrict__ rows4, FanGeo<float> gg, Dims d, QuarterMaps qm,

@@ -92,7 +92,7 @@ def test_host_only_entry_points(library):
     q.Ny = 9
     assert forward_rc(4, turn) == 1  # not square
     # scratch of the orbit kernels (float32 single slices): the forward's
-    # float4 per pixel (from 48 Mi pixel-angles per projection), the
+    # float4 per pixel (from 16 Mi pixel-angles per projection), the
     # backprojection's float4 per base angle and bin (even sides with cyclic
     # maps, from 12 Mi pixel-angles); the larger of the two
     work = lib.gr_work_bytes
@@ -108,7 +108,8 @@ def test_host_only_entry_points(library):
     # holds a 4-float4 geometry record per base angle)
     assert sized(512, 768, 360) == max(512 * 512 * 16, 90 * (768 + 3 + 4) * 16)
     assert sized(512, 4000, 400) == 100 * (4000 + 3 + 4) * 16
-    assert sized(256, 384, 360) == 90 * (384 + 3 + 4) * 16  # the backprojection's only
+    assert sized(256, 384, 360) == 256 * 256 * 16  # both copies, the forward's the larger
+    assert sized(192, 288, 360) == 90 * (288 + 3 + 4) * 16  # the backprojection's only
     assert sized(128, 192, 360) == 0
     # stacks (from 256 * 2^20 pixel-angles per slice): one slice's copy per
     # slice, up to 8 slices per launch pair; smaller slices keep the

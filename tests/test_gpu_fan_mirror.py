@@ -23,7 +23,7 @@ from tests.helpers import device_settings, host_settings, rel_l2
 
 pytestmark = pytest.mark.gpu
 
-# at least 48 * 2^20 pixel-angles per slice: the forward reads the orbit copy
+# at least 16 * 2^20 pixel-angles per slice: the forward reads the orbit copy
 BENCH = dict(geometry="fanbeam", img_shape=(512, 512), angles=360, n_detectors=768,
              detector_width=400.0, R=400.0, RE=200.0)
 CFGS = {

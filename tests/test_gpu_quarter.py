@@ -118,7 +118,7 @@ def _raw(ps, fwd, data_np, work, work_bytes, cuda_device, mirror=True):
 
 
 # sizes at which the orbit kernels work from interleaved scratch copies
-# (48 * 2^20 pixel-angles for the forward, 12 * 2^20 for the backprojection)
+# (16 * 2^20 pixel-angles for the forward, 12 * 2^20 for the backprojection)
 COPY_CFGS = {
     "copy_even": dict(geometry="fanbeam", img_shape=(360, 360), angles=480, n_detectors=540,
                       detector_width=400.0, R=400.0, RE=200.0),
