@@ -992,6 +992,36 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
         // second of an odd count is masked (its reciprocal set to zero adds
         // zeros).  t and ss advance by the same additions as one candidate
         // per trip.
+        if constexpr (MIRROR) {
+          // one candidate per trip: its two loads (P and M P) in flight and
+          // 80 registers instead of 94 (two per trip: 512^2 x 360 equal,
+          // 1024^2 x 720 387.5 against 382.2 us, 2048^2 x 1440 2618
+          // against 2592 us); the same sums bit for bit
+          for (int x = xlo; x <= xhi; ++x) {
+            const float4 pa = __ldg(img4 + o0);
+            const float4 qa = __ldg(img4 + oM);
+            const float ra = rcp_approx(t);
+            const float ua = fmaf(ss, ra, -s_mid0);
+            const float2 ra2 = make_float2(ra, ra);
+            const float2 a01 = __fmul2_rn(make_float2(pa.x, pa.y), ra2);
+            const float2 a23 = __fmul2_rn(make_float2(pa.z, pa.w), ra2);
+            const float2 ma01 = __fmul2_rn(make_float2(qa.x, qa.y), ra2);
+            const float2 ma23 = __fmul2_rn(make_float2(qa.z, qa.w), ra2);
+#pragma unroll
+            for (int q = 0; q < kRayGroup; ++q) {
+              const float wa = fmaxf(0.0f, 1.0f - fabsf((float)q - ua));
+              const float2 wa2 = make_float2(wa, wa);
+              acc01[q] = __ffma2_rn(wa2, a01, acc01[q]);
+              acc23[q] = __ffma2_rn(wa2, a23, acc23[q]);
+              macc01[q] = __ffma2_rn(wa2, ma01, macc01[q]);
+              macc23[q] = __ffma2_rn(wa2, ma23, macc23[q]);
+            }
+            o0 += stp;
+            oM += Mstep_x;
+            t += ddx;
+            ss += dx;
+          }
+        } else
         for (int x = xlo; x <= xhi; x += 2) {
           const bool two = x < xhi;
           const float tb = t + ddx, sb = ss + dx;
@@ -1903,8 +1933,9 @@ radon_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs, D
   }
 }
 
-// (The mirrored kernel at 94 registers; capped at 80 for 6 blocks per SM it
-// spilled and ran 512^2 x 360 in 99.4 instead of 77.0 us.)
+// (The mirrored kernel with two candidates per trip at 94 registers, capped
+// at 80 for 6 blocks per SM, spilled and ran 512^2 x 360 in 99.4 instead of
+// 77.0 us.)
 template <int SO, int IO, int SPLIT, bool PIX4, bool MIRROR, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
 fan_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4,
