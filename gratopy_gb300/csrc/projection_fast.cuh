@@ -532,6 +532,20 @@ __device__ __forceinline__ void row_range(float a_lo, float b_lo, float a_hi, fl
   y1 = min(n - 1, (int)ceilf(hi) + 1);
 }
 
+// Output oi of a lane group's R x C sums (acc[oi / C][oi % C]) picked by
+// selects, so that the lanes of a group, each with its own oi, run one
+// instruction stream (the epilogue's loads and stores of the group's outputs
+// then go out together instead of one lane's one after another).
+template <int R, int C>
+__device__ __forceinline__ float pick_output(const float (&acc)[R][C], int oi) {
+  float v = 0.0f;
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int c = 0; c < C; ++c) v = (oi == r * C + c) ? acc[r][c] : v;
+  return v;
+}
+
 template <int SO, int IO, int ZB, int SPLIT, class Epi>
 __device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ img, const float* __restrict__ ofs, RadonGeo<float> g,
                Dims d, Epi epi, uint3 bid) {
@@ -626,17 +640,20 @@ __device__ __forceinline__ double radon_fwd_fast_tile(const float* __restrict__ 
 #pragma unroll
     for (int r = 0; r < kRayGroup; ++r) warp_reduce_rows<SPLIT>(acc[r]);
   }
+  // every lane of the group now holds every sum: the lanes share the
+  // group's outputs, one each per round
+  constexpr int kN = kRayGroup * ZB;
   double part = 0.0;
-  if (active && L.lane_group == 0) {
+  if (active) {
     const float scale = g.delta_x * g.delta_x / g.delta_xi;
 #pragma unroll
-    for (int r = 0; r < kRayGroup; ++r) {
-      const int64_t s = s0 + r;
-      if (s < d.Ns) {
-#pragma unroll
-        for (int k = 0; k < ZB; ++k)
-          if (k < zn) part += epi(s, a, z0 + k, sino_index<SO>(s, a, z0 + k, d), acc[r][k] * scale);
-      }
+    for (int base = 0; base < kN; base += SPLIT) {
+      const int oi = base + L.lane_group;
+      const float v = pick_output<kRayGroup, ZB>(acc, oi);
+      const int64_t s = s0 + oi / ZB;
+      const int k = oi % ZB;
+      if (oi < kN && s < d.Ns && k < zn)
+        part += epi(s, a, z0 + k, sino_index<SO>(s, a, z0 + k, d), v * scale);
     }
   }
   return part;
@@ -760,16 +777,20 @@ __device__ __forceinline__ double fan_fwd_fast_tile(const float* __restrict__ im
 #pragma unroll
     for (int r = 0; r < kRayGroup; ++r) warp_reduce_rows<SPLIT>(acc[r]);
   }
+  // every lane of the group now holds every sum: the lanes share the
+  // group's outputs, one each per round
+  constexpr int kN = kRayGroup * ZB;
   double part = 0.0;
-  if (active && L.lane_group == 0) {
+  if (active) {
 #pragma unroll
-    for (int q = 0; q < kRayGroup; ++q) {
-      const int64_t s = s0 + q;
-      if (s < d.Ns) {
+    for (int base = 0; base < kN; base += SPLIT) {
+      const int oi = base + L.lane_group;
+      const float v = pick_output<kRayGroup, ZB>(acc, oi);
+      const int64_t s = s0 + oi / ZB;
+      const int k = oi % ZB;
+      if (oi < kN && s < d.Ns && k < zn) {
         const float sc = sdpd[s] / g.delta_xi * g.delta_x / R;
-#pragma unroll
-        for (int k = 0; k < ZB; ++k)
-          if (k < zn) part += epi(s, a, z0 + k, sino_index<SO>(s, a, z0 + k, d), acc[q][k] * sc);
+        part += epi(s, a, z0 + k, sino_index<SO>(s, a, z0 + k, d), v * sc);
       }
     }
   }
@@ -807,6 +828,7 @@ fan_fwd_fast(const float* __restrict__ img, const float* __restrict__ ofs,
 // angles differ by 360/Na degrees).  Within a warp, 32 / SPLIT groups of
 // SPLIT lanes each own kRayGroup adjacent bins.
 constexpr int kQuarterAnglesPerBlock = 2;
+
 
 template <int SPLIT>
 struct QuarterLayout {
@@ -1105,35 +1127,33 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
 #pragma unroll
     for (int m = 0; m < kOut; ++m) warp_reduce_rows<SPLIT>(acc[m]);
   }
+  // every lane of the group now holds every sum: the lanes share the
+  // group's outputs, one each per round
+  constexpr int kN = kOut * kRayGroup;
+  static_assert(kN % SPLIT == 0 || SPLIT > kN, "whole rounds of outputs");
   double part = 0.0;
-  if (active && L.lane_group == 0) {
+  if (active) {
     const int64_t mirror_max = d.Ns - 1 - Hs;  // mirrored outputs for s <= this
 #pragma unroll
-    for (int q = 0; q < kRayGroup; ++q) {
-      const int64_t s = s0 + q;
-      if (s < Hs) {
-        const float sc = sdpd[s] / g.delta_xi * g.delta_x / R;
-#pragma unroll
-        for (int m = 0; m < kOrbit; ++m) {
-          const int64_t am = a + ((m + shift) & (kOrbit - 1)) * quarter;
-          part += epi(s, am, z, sino_index<SO>(s, am, z, d), acc[m][q] * sc);
-        }
-        if constexpr (MIRROR) {
-          if (s <= mirror_max) {
-            // component k of the entry at M P is member m = -k mod 4: the
-            // output (Ns - 1 - s, c0 - (a + ((m + shift) mod 4) Q))
-            const int64_t sm = d.Ns - 1 - s;
-            const float scm = sdpd[sm] / g.delta_xi * g.delta_x / R;
-#pragma unroll
-            for (int k = 0; k < kOrbit; ++k) {
-              const int m = (kOrbit - k) & (kOrbit - 1);
-              const int64_t am = a + ((m + shift) & (kOrbit - 1)) * quarter;
-              int64_t bm = qm.mirror_pair - am;
-              if (bm < 0) bm += d.Na;
-              part += epi(sm, bm, z, sino_index<SO>(sm, bm, z, d), acc[kOrbit + k][q] * scm);
-            }
-          }
-        }
+    for (int base = 0; base < kN; base += SPLIT) {
+      const int oi = base + L.lane_group;
+      const float v = pick_output<kOut, kRayGroup>(acc, oi);
+      const int m = oi / kRayGroup;
+      const int64_t s = s0 + oi % kRayGroup;
+      // component k = m - 4 of the entry at M P is member -k mod 4: the
+      // output (Ns - 1 - s, c0 - (a + ((-k + shift) mod 4) Q))
+      const bool mir = MIRROR && m >= kOrbit;
+      const int mm = mir ? (kOrbit - (m - kOrbit)) & (kOrbit - 1) : m;
+      const int64_t am = a + ((mm + shift) & (kOrbit - 1)) * quarter;
+      int64_t bin = s, ang = am;
+      if (mir) {
+        bin = d.Ns - 1 - s;
+        ang = qm.mirror_pair - am;
+        if (ang < 0) ang += d.Na;
+      }
+      if (oi < kN && s < Hs && (!mir || s <= mirror_max)) {
+        const float sc = sdpd[bin] / g.delta_xi * g.delta_x / R;
+        part += epi(bin, ang, z, sino_index<SO>(bin, ang, z, d), v * sc);
       }
     }
   }
@@ -1704,23 +1724,28 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float* __restrict
 #pragma unroll
     for (int m = 0; m < kOrbit; ++m) warp_reduce_rows<SPLIT>(acc[m]);
   }
+  // every lane of the group now holds every sum.  Epilogues that read memory
+  // (solver steps) share the group's outputs over its lanes, one each per
+  // round, so their loads go out together; the plain store stays with the
+  // group's first lane (spread, 256^2 x 180 measured 2 us slower a step)
+  constexpr int kN = kOrbit * kRayGroup;
+  constexpr bool kSpread = !std::is_same<Epi, FwdStore<float>>::value;
+  constexpr int kLanes = kSpread ? SPLIT : 1;
+  static_assert(kN % SPLIT == 0 || SPLIT > kN, "whole rounds of outputs");
   double part = 0.0;
-  if (active && L.lane_group == 0) {
+  if (active && (kSpread || L.lane_group == 0)) {
     const float scale = g.delta_x * g.delta_x / g.delta_xi;
     const int64_t mirror_max = d.Ns - 1 - H;  // mirrored outputs for s <= this
 #pragma unroll
-    for (int q = 0; q < kRayGroup; ++q) {
-      const int64_t s = s0 + q;
-      if (s < H) {
-#pragma unroll
-        for (int m = 0; m < kOrbit; ++m) {
-          const int c = (m + shift) & (kOrbit - 1);
-          if ((c & 2) && s > mirror_max) continue;
-          const int64_t bin = (c & 2) ? d.Ns - 1 - s : s;
-          const int64_t ang = k + ((c & 1) ? Q : 0);
-          part += epi(bin, ang, z, sino_index<SO>(bin, ang, z, d), acc[m][q] * scale);
-        }
-      }
+    for (int base = 0; base < kN; base += kLanes) {
+      const int oi = base + (kSpread ? L.lane_group : 0);
+      const float v = pick_output<kOrbit, kRayGroup>(acc, oi);
+      const int64_t s = s0 + oi % kRayGroup;
+      const int c = (oi / kRayGroup + shift) & (kOrbit - 1);
+      const int64_t bin = (c & 2) ? d.Ns - 1 - s : s;
+      const int64_t ang = k + ((c & 1) ? Q : 0);
+      if (oi < kN && s < H && !((c & 2) && s > mirror_max))
+        part += epi(bin, ang, z, sino_index<SO>(bin, ang, z, d), v * scale);
     }
   }
   return part;
