@@ -1298,6 +1298,62 @@ orbit_rows(const float* __restrict__ sino, const float* __restrict__ sdpd,
   copy[a * nrow + e] = v;
 }
 
+// The epilogue of an orbit backprojection, whose thread owns the four pixels
+// of an orbit: with G > 1 angle groups the groups' sums meet in shared
+// memory and group j finishes members j, j + G, ... (each member's sum added
+// in the fixed group order), so up to four members' epilogues -- and their
+// loads -- run on different threads at once instead of one after another on
+// the first group's thread.  pixel(k, x, y) gives member k's pixel.
+template <int IO, int G, class Epi, class Pix>
+__device__ __forceinline__ double orbit_epilogue(const float (&sum)[4], bool own, Pix pixel,
+                                                 const Epi& epi, int64_t z, const Dims& d) {
+  constexpr int kOrbit = 4;
+  constexpr int kRowsT = kBwdTileSlow / G;
+  const int lane = threadIdx.x, trow = threadIdx.y;
+  double part = 0.0;
+  if constexpr (G > 1) {
+    const int grp = trow / kRowsT, trow_t = trow % kRowsT;
+    __shared__ float cred[kBwdTileSlow][kOrbit][kBwdTileFast];
+#pragma unroll
+    for (int k = 0; k < kOrbit; ++k) cred[trow][k][lane] = sum[k];
+    __syncthreads();
+#pragma unroll
+    for (int k0 = 0; k0 < kOrbit; k0 += G) {
+      const int k = k0 + grp;
+      if (own && k < kOrbit) {
+        float t = cred[trow_t][k][lane];
+#pragma unroll
+        for (int q = 1; q < G; ++q) t += cred[trow_t + q * kRowsT][k][lane];
+        int x, y;
+        pixel(k, x, y);
+        part += epi(x, y, z, img_index<IO>(x, y, z, d), t);
+      }
+    }
+  } else {
+    if (own) {
+#pragma unroll
+      for (int k = 0; k < kOrbit; ++k) {
+        int x, y;
+        pixel(k, x, y);
+        part += epi(x, y, z, img_index<IO>(x, y, z, d), sum[k]);
+      }
+    }
+  }
+  return part;
+}
+
+// Member k of four pixels held in arrays, by selects (no local memory).
+__device__ __forceinline__ void pick_pixel(const int (&ox)[4], const int (&oy)[4], int k, int& x,
+                                           int& y) {
+  x = ox[0];
+  y = oy[0];
+#pragma unroll
+  for (int m = 1; m < 4; ++m) {
+    x = k == m ? ox[m] : x;
+    y = k == m ? oy[m] : y;
+  }
+}
+
 // Backprojection over quarter-turn pixel orbits.  With the maps powers of
 // one quarter turn A (A_m = A^m about the image centre, N even) the pixels
 // P_k = A^k P_0 satisfy u(a + j Na/4, P_k) = u(a, P_{k-j mod 4}) for the
@@ -1402,29 +1458,9 @@ __device__ __forceinline__ double fan_bwd_orbit_tile(const float* __restrict__ s
       }
     }
   }
-  // fixed-order combination of the G angle groups
-  if constexpr (G > 1) {
-    __shared__ float cred[kBwdTileSlow][kOrbit][kBwdTileFast];
-#pragma unroll
-    for (int k = 0; k < kOrbit; ++k) cred[trow][k][lane] = acc[k];
-    __syncthreads();
-    if (grp == 0) {
-#pragma unroll
-      for (int k = 0; k < kOrbit; ++k) {
-        float t = cred[trow][k][lane];
-#pragma unroll
-        for (int q = 1; q < G; ++q) t += cred[trow + q * kRowsT][k][lane];
-        acc[k] = t;
-      }
-    }
-  }
-  double part = 0.0;
-  if (own && grp == 0) {
-#pragma unroll
-    for (int k = 0; k < kOrbit; ++k)
-      part += epi(ox[k], oy[k], z, img_index<IO>(ox[k], oy[k], z, d), acc[k]);
-  }
-  return part;
+  // fixed-order combination of the G angle groups, and the epilogue
+  return orbit_epilogue<IO, G>(
+      acc, own, [&](int k, int& x, int& y) { pick_pixel(ox, oy, k, x, y); }, epi, z, d);
 }
 
 template <int IO, int SO, int G, class Epi>
@@ -1561,30 +1597,15 @@ fan_bwd_orbit_rows(const float4* __restrict__ rows4, FanGeo<float> gg, Dims d, Q
     }
   }
   float sum[kOrbit] = {e01.x + o30.y, e01.y + o12.x, e23.x + o12.y, e23.y + o30.x};
-  // fixed-order combination of the G angle groups
-  if constexpr (G > 1) {
-    __shared__ float cred[kBwdTileSlow][kOrbit][kBwdTileFast];
-#pragma unroll
-    for (int k = 0; k < kOrbit; ++k) cred[trow][k][lane] = sum[k];
-    __syncthreads();
-    if (grp == 0) {
-#pragma unroll
-      for (int k = 0; k < kOrbit; ++k) {
-        float t = cred[trow][k][lane];
-#pragma unroll
-        for (int q = 1; q < G; ++q) t += cred[trow + q * kRowsT][k][lane];
-        sum[k] = t;
-      }
-    }
-  }
-  double part = 0.0;
-  if (own && grp == 0) {
-    int ox[kOrbit], oy[kOrbit];
-    orbit(ox, oy);
-#pragma unroll
-    for (int k = 0; k < kOrbit; ++k)
-      part += epi(ox[k], oy[k], z, img_index<IO>(ox[k], oy[k], z, d), sum[k]);
-  }
+  // fixed-order combination of the G angle groups, and the epilogue
+  const double part = orbit_epilogue<IO, G>(
+      sum, own,
+      [&](int k, int& x, int& y) {
+        int ox[kOrbit], oy[kOrbit];
+        orbit(ox, oy);
+        pick_pixel(ox, oy, k, x, y);
+      },
+      epi, z, d);
   if (Epi::kReduce) {
     const double t = block_sum(part, red);
     if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
@@ -1897,31 +1918,16 @@ __device__ __forceinline__ double radon_bwd_orbit_tile(const float4* __restrict_
     C = __ffma2_rn(W, lo[1], C);
     D = __ffma2_rn(W, hi2[1], D);
   }
-  float sum[kOrbit] = {A.x + C.y, B.y + C.x, B.x + D.y, A.y + D.x};
-  if constexpr (G > 1) {
-    __shared__ float cred[kBwdTileSlow][kOrbit][kBwdTileFast];
-#pragma unroll
-    for (int m = 0; m < kOrbit; ++m) cred[trow][m][lane] = sum[m];
-    __syncthreads();
-    if (grp == 0) {
-#pragma unroll
-      for (int m = 0; m < kOrbit; ++m) {
-        float t = cred[trow][m][lane];
-#pragma unroll
-        for (int q = 1; q < G; ++q) t += cred[trow + q * kRowsT][m][lane];
-        sum[m] = t;
-      }
-    }
-  }
-  double part = 0.0;
-  if (own && grp == 0) {
-    int ox[kOrbit], oy[kOrbit];
-    orbit(ox, oy);
-#pragma unroll
-    for (int m = 0; m < kOrbit; ++m)
-      part += epi(ox[m], oy[m], z, img_index<IO>(ox[m], oy[m], z, d), sum[m]);
-  }
-  return part;
+  const float sum[kOrbit] = {A.x + C.y, B.y + C.x, B.x + D.y, A.y + D.x};
+  // fixed-order combination of the G angle groups, and the epilogue
+  return orbit_epilogue<IO, G>(
+      sum, own,
+      [&](int k, int& x, int& y) {
+        int ox[kOrbit], oy[kOrbit];
+        orbit(ox, oy);
+        pick_pixel(ox, oy, k, x, y);
+      },
+      epi, z, d);
 }
 
 // From the row copy: slice z0 + blockIdx.z, its copy is copy blockIdx.z.
