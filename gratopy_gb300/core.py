@@ -346,7 +346,10 @@ class ProjectionSettings:
         ga = _lib.GrGeometry.from_buffer_copy(g)
         ga.ofs = tables["ofs_adj"].data_ptr()
         self._geom_adj[dtype] = ga
-        self._work_bytes[dtype] = int(_lib.raw("gr_work_bytes")(ctypes.byref(g), 1))
+        # a slice's copies, or two slices' where a stack's orbit forward takes
+        # slices in pairs
+        work = _lib.raw("gr_work_bytes")
+        self._work_bytes[dtype] = max(int(work(ctypes.byref(g), 1)), int(work(ctypes.byref(g), 2)))
 
     def quarter_maps(self):
         """Index maps of the geometry's orbit symmetry (see

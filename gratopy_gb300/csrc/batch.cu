@@ -155,7 +155,7 @@ __device__ __forceinline__ double fwd_orbit_item(const gr_batch_problem& P, int 
     RadonGeo<float> g;
     g.delta_x = P.geo[0];
     g.delta_xi = P.geo[1];
-    return fast::radon_fwd_quarter_tile<ORDER_F, ORDER_F, 4 * SPLIT, false, BatchFwdEpi>(
+    return fast::radon_fwd_quarter_tile<ORDER_F, ORDER_F, 4 * SPLIT, false, 1, BatchFwdEpi>(
         in, nullptr, P.ofs, g, dims2(P), qm, e, bid, 0);
   } else {
     return fast::fan_fwd_quarter_tile<ORDER_F, ORDER_F, 2 * SPLIT, false, false, BatchFwdEpi>(

@@ -420,7 +420,7 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
         if (chunk == 0) {
           // no copy: the four orbit members gathered from the image
           for (int64_t z = 0; z < Nz; ++z)
-            fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, false, Epi><<<sgrid, kFwdBlock, 0, st>>>(
+            fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, false, 1, Epi><<<sgrid, kFwdBlock, 0, st>>>(
                 img + z * sz, nullptr, ofs, radon_geo<float>(g->geo), d, qm, epi,
                 partials ? partials + z * per_slice_blocks : nullptr, skip, z);
           return check_launch();
@@ -440,11 +440,18 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
             const dim3 pgrid((g->Nx + 255) / 256, g->Ny, zc);
             fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, z0, skip);
           }
-          for (int c = 0; c < zc; ++c) {
+          // slices in pairs: a candidate's weights serve both slices' copies
+          for (int c = 0; c < zc; c += 2) {
             const int64_t z = z0 + c;
-            fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, true, Epi><<<sgrid, kFwdBlock, 0, st>>>(
-                img + z * sz, img4 + c * slice4, ofs, radon_geo<float>(g->geo), d, qm, epi,
-                partials ? partials + z * per_slice_blocks : nullptr, skip, z);
+            double* pz = partials ? partials + z * per_slice_blocks : nullptr;
+            if (c + 1 < zc)
+              fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, true, 2, Epi>
+                  <<<sgrid, kFwdBlock, 0, st>>>(img + z * sz, img4 + c * slice4, ofs,
+                                                radon_geo<float>(g->geo), d, qm, epi, pz, skip, z);
+            else
+              fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, true, 1, Epi>
+                  <<<sgrid, kFwdBlock, 0, st>>>(img + z * sz, img4 + c * slice4, ofs,
+                                                radon_geo<float>(g->geo), d, qm, epi, pz, skip, z);
           }
         }
         return check_launch();

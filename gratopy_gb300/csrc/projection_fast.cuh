@@ -1636,8 +1636,10 @@ __device__ __forceinline__ int radon_orbit_half(int64_t Ns) { return (int)((Ns +
 // Two candidates per trip, packed pair sums, branch-free hat weights, as in
 // fan_fwd_quarter.  PIX4: the four members of a pixel's orbit come from the
 // orbit copy (one 16-byte load); otherwise from the slice `img` itself
-// through the maps (four loads).
-template <int SO, int IO, int SPLIT, bool PIX4, class Epi>
+// through the maps (four loads).  ZS = 2 (with the copy): slices z and z + 1
+// at once, the second slice's copy following the first's; a candidate's
+// four hat weights then serve both slices' members, one candidate per trip.
+template <int SO, int IO, int SPLIT, bool PIX4, int ZS, class Epi>
 __device__ __forceinline__ double radon_fwd_quarter_tile(const float* __restrict__ img,
                                                          const float4* __restrict__ img4,
                                                          const float* __restrict__ ofs,
@@ -1645,6 +1647,7 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float* __restrict
                                                          QuarterMaps qm, Epi epi, uint3 bid,
                                                          int64_t z) {
   constexpr int kOrbit = 4;
+  static_assert(ZS == 1 || (ZS == 2 && PIX4), "two slices from the orbit copies");
   const QuarterLayout<SPLIT> L(bid);
   const int64_t s0 = L.s0;
   const int64_t k = L.a;
@@ -1652,8 +1655,11 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float* __restrict
   const int H = radon_orbit_half(d.Ns);
   const bool active = s0 < H && k < Q;
   float2 acc01[kRayGroup], acc23[kRayGroup];
+  float2 zacc01[ZS == 2 ? kRayGroup : 1], zacc23[ZS == 2 ? kRayGroup : 1];  // slice z + 1
 #pragma unroll
   for (int q = 0; q < kRayGroup; ++q) acc01[q] = acc23[q] = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int q = 0; q < (ZS == 2 ? kRayGroup : 1); ++q) zacc01[q] = zacc23[q] = make_float2(0.f, 0.f);
   int shift = 0;
   if (active) {
     int64_t ab = k;
@@ -1697,6 +1703,26 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float* __restrict
       const int yhi = min(N - 1, (int)floorf(fmaf(bx, xf, ahi)));
       float pos = fmaf(Y, (float)ylo, fmaf(X, xf, base));
       int o0 = ylo * sy + x * sx;
+      if constexpr (ZS == 2) {
+        // both slices' members, one candidate per trip
+        const int64_t slice4 = (int64_t)N * N;
+        for (int y = ylo; y <= yhi; ++y) {
+          const float4 pa4 = __ldg(img4 + o0);
+          const float4 qa4 = __ldg(img4 + slice4 + o0);
+#pragma unroll
+          for (int q = 0; q < kRayGroup; ++q) {
+            const float wa = fmaxf(0.0f, 1.0f - fabsf(pos - (float)q));
+            const float2 wa2 = make_float2(wa, wa);
+            acc01[q] = __ffma2_rn(wa2, make_float2(pa4.x, pa4.y), acc01[q]);
+            acc23[q] = __ffma2_rn(wa2, make_float2(pa4.z, pa4.w), acc23[q]);
+            zacc01[q] = __ffma2_rn(wa2, make_float2(qa4.x, qa4.y), zacc01[q]);
+            zacc23[q] = __ffma2_rn(wa2, make_float2(qa4.z, qa4.w), zacc23[q]);
+          }
+          o0 += sy;
+          pos += Y;
+        }
+        continue;
+      }
       int om[3];
 #pragma unroll
       for (int m = 0; m < 3; ++m) om[m] = mbase[m] + x * mstep_x[m] + ylo * mstep_y[m];
@@ -1733,23 +1759,30 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float* __restrict
       }
     }
   }
-  float acc[kOrbit][kRayGroup];
+  constexpr int kOut = kOrbit * ZS;  // members of slice z, then of slice z + 1
+  float acc[kOut][kRayGroup];
 #pragma unroll
   for (int q = 0; q < kRayGroup; ++q) {
     acc[0][q] = acc01[q].x;
     acc[1][q] = acc01[q].y;
     acc[2][q] = acc23[q].x;
     acc[3][q] = acc23[q].y;
+    if constexpr (ZS == 2) {
+      acc[4][q] = zacc01[q].x;
+      acc[5][q] = zacc01[q].y;
+      acc[6][q] = zacc23[q].x;
+      acc[7][q] = zacc23[q].y;
+    }
   }
   if (SPLIT > 1) {
 #pragma unroll
-    for (int m = 0; m < kOrbit; ++m) warp_reduce_rows<SPLIT>(acc[m]);
+    for (int m = 0; m < kOut; ++m) warp_reduce_rows<SPLIT>(acc[m]);
   }
   // every lane of the group now holds every sum.  Epilogues that read memory
   // (solver steps) share the group's outputs over its lanes, one each per
   // round, so their loads go out together; the plain store stays with the
   // group's first lane (spread, 256^2 x 180 measured 2 us slower a step)
-  constexpr int kN = kOrbit * kRayGroup;
+  constexpr int kN = kOut * kRayGroup;
   constexpr bool kSpread = !std::is_same<Epi, FwdStore<float>>::value;
   constexpr int kLanes = kSpread ? SPLIT : 1;
   static_assert(kN % SPLIT == 0 || SPLIT > kN, "whole rounds of outputs");
@@ -1760,20 +1793,25 @@ __device__ __forceinline__ double radon_fwd_quarter_tile(const float* __restrict
 #pragma unroll
     for (int base = 0; base < kN; base += kLanes) {
       const int oi = base + (kSpread ? L.lane_group : 0);
-      const float v = pick_output<kOrbit, kRayGroup>(acc, oi);
+      const float v = pick_output<kOut, kRayGroup>(acc, oi);
       const int64_t s = s0 + oi % kRayGroup;
-      const int c = (oi / kRayGroup + shift) & (kOrbit - 1);
+      const int m = oi / kRayGroup;
+      const int64_t zz = z + m / kOrbit;
+      const int c = (m + shift) & (kOrbit - 1);
       const int64_t bin = (c & 2) ? d.Ns - 1 - s : s;
       const int64_t ang = k + ((c & 1) ? Q : 0);
       if (oi < kN && s < H && !((c & 2) && s > mirror_max))
-        part += epi(bin, ang, z, sino_index<SO>(bin, ang, z, d), v * scale);
+        part += epi(bin, ang, zz, sino_index<SO>(bin, ang, zz, d), v * scale);
     }
   }
   return part;
 }
 
-// One launch per slice: img points at slice z, img4 at its orbit copy (PIX4).
-template <int SO, int IO, int SPLIT, bool PIX4, class Epi>
+// One launch per slice (ZS = 2: per pair of slices): img points at slice z,
+// img4 at its orbit copy (PIX4).  A pair's block partial covers both slices
+// and lands in slice z's slot; slice z + 1's slot gets 0, so the partials of
+// a stack keep one slot per block and slice.
+template <int SO, int IO, int SPLIT, bool PIX4, int ZS, class Epi>
 __global__ void __launch_bounds__(kFwdBlock)
 radon_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4,
                   const float* __restrict__ ofs, RadonGeo<float> g, Dims d, QuarterMaps qm,
@@ -1781,11 +1819,14 @@ radon_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4
                   int64_t z) {
   __shared__ double red[32];
   if (skip != nullptr && *skip) return;
-  const double part = radon_fwd_quarter_tile<SO, IO, SPLIT, PIX4, Epi>(img, img4, ofs, g, d, qm,
-                                                                       epi, blockIdx, z);
+  const double part = radon_fwd_quarter_tile<SO, IO, SPLIT, PIX4, ZS, Epi>(
+      img, img4, ofs, g, d, qm, epi, blockIdx, z);
   if (Epi::kReduce) {
     const double t = block_sum(part, red);
-    if (threadIdx.x + blockDim.x * threadIdx.y == 0) partials[bid_linear()] = t;
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0) {
+      partials[bid_linear()] = t;
+      if (ZS == 2) partials[bid_linear() + (int64_t)gridDim.x * gridDim.y] = 0.0;
+    }
   }
 }
 

@@ -189,13 +189,14 @@ def test_radon_orbit_solvers(cuda_device):
 
 @pytest.mark.parametrize("io", ["F", "C"])
 @pytest.mark.parametrize("so", ["F", "C"])
-@pytest.mark.parametrize("copies", [0, 1, 8])
+@pytest.mark.parametrize("copies", [0, 1, 2, 8])
 def test_radon_orbit_stack(cuda_device, io, so, copies):
     """A 5-slice stack of 256^2 x 512 (2^25 pixel-angles per slice, the
     smallest that takes the orbit forward): scratch for 1 slice (one copy and
-    one forward per slice) or 8 (one copy of the 5 slices), against the
-    per-angle kernels and, for the Fortran pair, the float64 oracle; without
-    scratch the stack keeps the per-angle kernels.  The
+    one single-slice forward per slice), 2 (slices in pairs, the last one
+    alone) or 8 (one copy of the 5 slices), against the per-angle kernels
+    and, for the Fortran pair, the float64 oracle; without scratch the stack
+    keeps the per-angle kernels.  The
     fused reduction of CG's forward (block partials of <W q, q>, one slice's
     after another's) covers every partial exactly once."""
     import ctypes
@@ -209,17 +210,22 @@ def test_radon_orbit_stack(cuda_device, io, so, copies):
     ps = device_settings(cfg, cuda_device)
     dt = np.dtype("float32")
     assert ps.gr_geometry(dt).sym == 2
-    one = ps._work_bytes[dt]  # a single slice's: the larger, the backprojection's rows
-    assert one == 256 * (363 + 3) * 16 and one // (256 * 256 * 16) == 1
+    # the settings bind two slices' forward copies (the stack's pairs); one
+    # slice's is smaller than the single slice's backprojection rows
+    per_slice, rows = 256 * 256 * 16, 256 * (363 + 3) * 16
+    one = ps._work_bytes[dt]
+    assert one == 2 * per_slice
     rng = np.random.default_rng(31 + copies + 2 * (io == "C") + 4 * (so == "C"))
     img = rng.random(tuple(ps.img_shape) + (5,))
     saved = dict(ps._work)
+    nbytes = max(rows, per_slice * copies) if copies else 0
+    assert nbytes // per_slice == copies
     try:
-        ps._work_bytes[dt] = one * copies
+        ps._work_bytes[dt] = nbytes
         ps._work = {}
         orbit = _project(ps, True, img, io, so, cuda_device, work=copies > 0)
         if copies:
-            assert ps.gr_geometry(dt).work_bytes == one * copies
+            assert ps.gr_geometry(dt).work_bytes == nbytes
     finally:
         ps._work_bytes[dt] = one
         ps._work = saved
