@@ -1197,25 +1197,26 @@ orbit_pixels_tiled(const float* __restrict__ img, Dims d, QuarterMaps qm,
   static_assert(IO == ORDER_F, "x-fastest images only");
   __shared__ float tile[3][kOrbitTile][kOrbitTile + 1];
   if (skip != nullptr && *skip) return;
+  // offsets within a slice in 32 bits (the orbit kernels' slices hold fewer
+  // than 2^31 pixels): a quarter of the 64-bit form's index arithmetic
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int64_t X0 = (int64_t)blockIdx.x * kOrbitTile, Y0 = (int64_t)blockIdx.y * kOrbitTile;
-  const int64_t z = z0 + blockIdx.z;
-  const int64_t Nx = d.Nx, Ny = d.Ny;
-  const float* slice = img + z * Nx * Ny;
-  int64_t rx0[3], ry0[3];
+  const int X0 = (int)blockIdx.x * kOrbitTile, Y0 = (int)blockIdx.y * kOrbitTile;
+  const int Nx = (int)d.Nx, Ny = (int)d.Ny;
+  const float* slice = img + (z0 + blockIdx.z) * (int64_t)Nx * Ny;
+  int rx0[3], ry0[3];
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
     // the turned tile: the images of two opposite corners bound it
-    const int64_t ax = qm.cx[m] + qm.axx[m] * X0 + qm.axy[m] * Y0;
-    const int64_t ay = qm.cy[m] + qm.ayx[m] * X0 + qm.ayy[m] * Y0;
-    const int64_t bx = ax + (qm.axx[m] + qm.axy[m]) * (kOrbitTile - 1);
-    const int64_t by = ay + (qm.ayx[m] + qm.ayy[m]) * (kOrbitTile - 1);
+    const int ax = qm.cx[m] + qm.axx[m] * X0 + qm.axy[m] * Y0;
+    const int ay = qm.cy[m] + qm.ayx[m] * X0 + qm.ayy[m] * Y0;
+    const int bx = ax + (qm.axx[m] + qm.axy[m]) * (kOrbitTile - 1);
+    const int by = ay + (qm.ayx[m] + qm.ayy[m]) * (kOrbitTile - 1);
     rx0[m] = ax < bx ? ax : bx;
     ry0[m] = ay < by ? ay : by;
-    const int64_t x = rx0[m] + tx, y = ry0[m] + ty;
+    const int x = rx0[m] + tx, y = ry0[m] + ty;
     if (x >= 0 && x < Nx && y >= 0 && y < Ny) tile[m][ty][tx] = ldg(slice + x + Nx * y);
   }
-  const int64_t x = X0 + tx, y = Y0 + ty;
+  const int x = X0 + tx, y = Y0 + ty;
   const bool in = x < Nx && y < Ny;
   const float v0 = in ? ldg(slice + x + Nx * y) : 0.0f;
   __syncthreads();
@@ -1223,11 +1224,11 @@ orbit_pixels_tiled(const float* __restrict__ img, Dims d, QuarterMaps qm,
   float v[3];
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
-    const int64_t mx = qm.cx[m] + qm.axx[m] * x + qm.axy[m] * y;
-    const int64_t my = qm.cy[m] + qm.ayx[m] * x + qm.ayy[m] * y;
+    const int mx = qm.cx[m] + qm.axx[m] * x + qm.axy[m] * y;
+    const int my = qm.cy[m] + qm.ayx[m] * x + qm.ayy[m] * y;
     v[m] = tile[m][my - ry0[m]][mx - rx0[m]];
   }
-  img4[((int64_t)blockIdx.z * Ny + y) * Nx + x] = make_float4(v0, v[0], v[1], v[2]);
+  img4[(int64_t)blockIdx.z * Nx * Ny + (y * Nx + x)] = make_float4(v0, v[0], v[1], v[2]);
 }
 
 // The four sinogram rows of every quarter-turn orbit of angles, premultiplied
