@@ -101,11 +101,15 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   __syncthreads();
   if (lane == 0) red[warp] = v;
   __syncthreads();
+  // the warps' sums by one more warp reduction (a fixed order, five
+  // dependent adds instead of one per warp)
   double t = 0.0;
-  if (tid == 0) {
-    for (int w = 0; w < nwarps; ++w) t += red[w];
+  if (warp == 0) {
+    t = lane < nwarps ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(full, t, o);
   }
-  return t;
+  return tid == 0 ? t : 0.0;
 }
 
 }  // namespace gr
