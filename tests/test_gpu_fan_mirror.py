@@ -32,6 +32,7 @@ CFGS = {
     "reversed": dict(BENCH, reverse_detector=True),
     "wide_fan": dict(BENCH, img_shape=(384, 384), angles=400, n_detectors=601, R=300.0,
                      RE=150.0, detector_width=500.0),
+    "odd_side": dict(BENCH, img_shape=(389, 389), angles=360, n_detectors=583),
 }
 
 
