@@ -90,6 +90,14 @@ __device__ __forceinline__ int64_t bid_linear() {
 // Deterministic block-wide sum of one double per thread.  Every thread of the
 // block must call it; the result is valid in thread 0.  `red` must hold one
 // double per warp.
+// Programmatic dependent launch (kernels launched by launch_pdl): wait until
+// the kernel before this one in the stream has completed and its writes are
+// visible (returns at once for a kernel launched without the attribute), and
+// let the next kernel start launching.  The wait is the hardware's, bounded
+// by the previous kernel's completion; it comes before any global access.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ double block_sum(double v, double* red) {
   const unsigned full = 0xffffffffu;
 #pragma unroll

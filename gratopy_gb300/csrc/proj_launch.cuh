@@ -493,8 +493,8 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
           if constexpr (IO == ORDER_F) {
             constexpr int kTile = fast::kOrbitTile;
             const dim3 tgrid((g->Nx + kTile - 1) / kTile, (g->Ny + kTile - 1) / kTile, zc);
-            fast::orbit_pixels_tiled<IO><<<tgrid, dim3(kTile, kTile), 0, st>>>(img, d, qm,
-                                                                               img4, z0, skip);
+            launch_pdl(fast::orbit_pixels_tiled<IO>, tgrid, dim3(kTile, kTile), st, img, d, qm,
+                       img4, (int64_t)z0, skip);
           } else {
             const dim3 pgrid((g->Nx + 255) / 256, g->Ny, zc);
             fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, z0, skip);
@@ -503,13 +503,13 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
             const int64_t z = z0 + k;
             double* pz = partials ? partials + z * per_slice_blocks : nullptr;
             if (mirror)  // half the bins: twice the lanes per group
-              fast::fan_fwd_quarter<SO, IO, 2 * kQSplit, true, true, Epi>
-                  <<<sgrid, kFwdBlock, 0, st>>>(img + z * sz, img4 + k * slice4, ofs, sdpd,
-                                                fan_geo<float>(g->geo), d, qm, epi, pz, skip, z);
+              launch_pdl(fast::fan_fwd_quarter<SO, IO, 2 * kQSplit, true, true, Epi>, sgrid,
+                         dim3(kFwdBlock), st, img + z * sz, img4 + k * slice4, ofs, sdpd,
+                         fan_geo<float>(g->geo), d, qm, epi, pz, skip, z);
             else
-              fast::fan_fwd_quarter<SO, IO, kQSplit, true, false, Epi>
-                  <<<sgrid, kFwdBlock, 0, st>>>(img + z * sz, img4 + k * slice4, ofs, sdpd,
-                                                fan_geo<float>(g->geo), d, qm, epi, pz, skip, z);
+              launch_pdl(fast::fan_fwd_quarter<SO, IO, kQSplit, true, false, Epi>, sgrid,
+                         dim3(kFwdBlock), st, img + z * sz, img4 + k * slice4, ofs, sdpd,
+                         fan_geo<float>(g->geo), d, qm, epi, pz, skip, z);
           }
         }
       } else {
@@ -590,11 +590,11 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
           const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;
           // one more block column writes the base angles' records
           const dim3 rgrid((g->Ns + fast::kOrbitRowPad + 255) / 256 + 1, g->Na / 4, zc);
-          fast::orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, sdpd, ofs, fan_geo<float>(g->geo), d,
-                                                      rows4, z0, skip);
-          fast::fan_bwd_orbit_rows<IO, SPLIT, Epi><<<dim3(grid.x, grid.y, zc), block, 0, st>>>(
-              rows4, fan_geo<float>(g->geo), d, quarter_maps(g), epi,
-              partials ? partials + z0 * per_slice_blocks : nullptr, skip, z0);
+          launch_pdl(fast::orbit_rows<SO>, rgrid, dim3(256), st, sino, sdpd, ofs,
+                     fan_geo<float>(g->geo), d, rows4, (int64_t)z0, skip);
+          launch_pdl(fast::fan_bwd_orbit_rows<IO, SPLIT, Epi>, dim3(grid.x, grid.y, zc), block, st,
+                     (const float4*)rows4, fan_geo<float>(g->geo), d, quarter_maps(g), epi,
+                     partials ? partials + z0 * per_slice_blocks : nullptr, skip, (int64_t)z0);
         }
       } else {
         fast::fan_bwd_orbit<IO, SO, SPLIT, Epi><<<grid, block, 0, st>>>(

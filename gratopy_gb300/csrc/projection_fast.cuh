@@ -1196,6 +1196,8 @@ orbit_pixels_tiled(const float* __restrict__ img, Dims d, QuarterMaps qm,
                    float4* __restrict__ img4, int64_t z0, const int* __restrict__ skip) {
   static_assert(IO == ORDER_F, "x-fastest images only");
   __shared__ float tile[3][kOrbitTile][kOrbitTile + 1];
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   // offsets within a slice in 32 bits (the orbit kernels' slices hold fewer
   // than 2^31 pixels): a quarter of the 64-bit form's index arithmetic
@@ -1275,6 +1277,8 @@ __global__ void __launch_bounds__(256)
 orbit_rows(const float* __restrict__ sino, const float* __restrict__ sdpd,
            const float* __restrict__ ofs, FanGeo<float> gg, Dims d, float4* __restrict__ rows4,
            int64_t z0, const int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const int64_t a = blockIdx.y;
   const int64_t nrow = d.Ns + kOrbitRowPad;
@@ -1511,6 +1515,8 @@ fan_bwd_orbit_rows(const float4* __restrict__ rows4, FanGeo<float> gg, Dims d, Q
   constexpr int kOrbit = 4;
   constexpr int kRowsT = kBwdTileSlow / G;  // quadrant rows of the block tile
   __shared__ double red[32];
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const int lane = threadIdx.x, trow = threadIdx.y;
   const int grp = trow / kRowsT, trow_t = trow % kRowsT;
@@ -2018,6 +2024,8 @@ fan_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4,
   // one launch per slice: img and img4 point at slice z (a base offset
   // computed here instead of taken from the parameters measured 8% slower)
   __shared__ double red[32];
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const double part = fan_fwd_quarter_tile<SO, IO, SPLIT, PIX4, MIRROR, Epi>(
       img, img4, ofs, sdpd, g, d, qm, epi, blockIdx, z);
