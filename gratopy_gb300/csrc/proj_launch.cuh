@@ -420,9 +420,9 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
         if (chunk == 0) {
           // no copy: the four orbit members gathered from the image
           for (int64_t z = 0; z < Nz; ++z)
-            fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, false, 1, Epi><<<sgrid, kFwdBlock, 0, st>>>(
-                img + z * sz, nullptr, ofs, radon_geo<float>(g->geo), d, qm, epi,
-                partials ? partials + z * per_slice_blocks : nullptr, skip, z);
+            launch_pdl(fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, false, 1, Epi>, sgrid,
+                       dim3(kFwdBlock), st, img + z * sz, nullptr, ofs, radon_geo<float>(g->geo),
+                       d, qm, epi, partials ? partials + z * per_slice_blocks : nullptr, skip, z);
           return check_launch();
         }
         // slices in chunks: each pixel's four orbit pixels as one float4,
@@ -434,24 +434,25 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
           if constexpr (IO == ORDER_F) {
             constexpr int kTile = fast::kOrbitTile;
             const dim3 tgrid((g->Nx + kTile - 1) / kTile, (g->Ny + kTile - 1) / kTile, zc);
-            fast::orbit_pixels_tiled<IO><<<tgrid, dim3(kTile, kTile), 0, st>>>(img, d, qm, img4,
-                                                                               z0, skip);
+            launch_pdl(fast::orbit_pixels_tiled<IO>, tgrid, dim3(kTile, kTile), st, img, d, qm,
+                       img4, (int64_t)z0, skip);
           } else {
             const dim3 pgrid((g->Nx + 255) / 256, g->Ny, zc);
-            fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, z0, skip);
+            launch_pdl(fast::orbit_pixels<IO>, pgrid, dim3(256), st, img, d, qm, img4,
+                       (int64_t)z0, skip);
           }
           // slices in pairs: a candidate's weights serve both slices' copies
           for (int c = 0; c < zc; c += 2) {
             const int64_t z = z0 + c;
             double* pz = partials ? partials + z * per_slice_blocks : nullptr;
             if (c + 1 < zc)
-              fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, true, 2, Epi>
-                  <<<sgrid, kFwdBlock, 0, st>>>(img + z * sz, img4 + c * slice4, ofs,
-                                                radon_geo<float>(g->geo), d, qm, epi, pz, skip, z);
+              launch_pdl(fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, true, 2, Epi>, sgrid,
+                         dim3(kFwdBlock), st, img + z * sz, (const float4*)(img4 + c * slice4),
+                         ofs, radon_geo<float>(g->geo), d, qm, epi, pz, skip, z);
             else
-              fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, true, 1, Epi>
-                  <<<sgrid, kFwdBlock, 0, st>>>(img + z * sz, img4 + c * slice4, ofs,
-                                                radon_geo<float>(g->geo), d, qm, epi, pz, skip, z);
+              launch_pdl(fast::radon_fwd_quarter<SO, IO, 4 * SPLIT, true, 1, Epi>, sgrid,
+                         dim3(kFwdBlock), st, img + z * sz, (const float4*)(img4 + c * slice4),
+                         ofs, radon_geo<float>(g->geo), d, qm, epi, pz, skip, z);
           }
         }
         return check_launch();
@@ -497,7 +498,8 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
                        img4, (int64_t)z0, skip);
           } else {
             const dim3 pgrid((g->Nx + 255) / 256, g->Ny, zc);
-            fast::orbit_pixels<IO><<<pgrid, 256, 0, st>>>(img, d, qm, img4, z0, skip);
+            launch_pdl(fast::orbit_pixels<IO>, pgrid, dim3(256), st, img, d, qm, img4,
+                       (int64_t)z0, skip);
           }
           for (int k = 0; k < zc; ++k) {
             const int64_t z = z0 + k;
@@ -514,7 +516,8 @@ int launch_fwd_zb(const gr_geometry* g, const T* img, int Nz, Epi epi, double* p
         }
       } else {
         for (int64_t z = 0; z < Nz; ++z)
-          fast::fan_fwd_quarter<SO, IO, kQSplit, false, false, Epi><<<sgrid, kFwdBlock, 0, st>>>(
+          launch_pdl(fast::fan_fwd_quarter<SO, IO, kQSplit, false, false, Epi>, sgrid,
+                     dim3(kFwdBlock), st,
               img + z * sz, nullptr, ofs, sdpd, fan_geo<float>(g->geo), d, qm, epi,
               partials ? partials + z * per_slice_blocks : nullptr, skip, z);
       }
@@ -597,8 +600,8 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
                      partials ? partials + z0 * per_slice_blocks : nullptr, skip, (int64_t)z0);
         }
       } else {
-        fast::fan_bwd_orbit<IO, SO, SPLIT, Epi><<<grid, block, 0, st>>>(
-            sino, ofs, sdpd, fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials, skip, 0);
+        launch_pdl(fast::fan_bwd_orbit<IO, SO, SPLIT, Epi>, grid, block, st, sino, ofs, sdpd,
+                   fan_geo<float>(g->geo), d, quarter_maps(g), epi, partials, skip, (int64_t)0);
       }
     } else if (use_radon_orbit_bwd(g, Nz)) {
       // half-circle orbits, slices in chunks: the mirror-interleaved row
@@ -606,18 +609,21 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
       float4* rows4 = static_cast<float4*>(g->work);
       const int chunk = work_slices(g, radon_orbit_bwd_bytes(g, Nz), Nz);
       if (chunk == 0) {
-        fast::radon_bwd_orbit<IO, SO, SPLIT, Epi><<<grid, block, 0, st>>>(
-            sino, static_cast<const float*>(g->ofs), d, quarter_maps(g), epi, partials, skip, 0);
+        launch_pdl(fast::radon_bwd_orbit<IO, SO, SPLIT, Epi>, grid, block, st, sino,
+                   static_cast<const float*>(g->ofs), d, quarter_maps(g), epi, partials, skip,
+                   (int64_t)0);
         return check_launch();
       }
       const int64_t per_slice_blocks = (int64_t)grid.x * grid.y;
       for (int z0 = 0; z0 < Nz; z0 += chunk) {
         const int zc = Nz - z0 < chunk ? Nz - z0 : chunk;
         const dim3 rgrid((g->Ns + fast::kOrbitRowPad + 255) / 256, g->Na / 2, zc);
-        fast::radon_orbit_rows<SO><<<rgrid, 256, 0, st>>>(sino, d, rows4, z0, skip);
-        fast::radon_bwd_orbit_rows<IO, SPLIT, Epi><<<dim3(grid.x, grid.y, zc), block, 0, st>>>(
-            rows4, static_cast<const float*>(g->ofs), d, quarter_maps(g), epi,
-            partials ? partials + z0 * per_slice_blocks : nullptr, skip, z0);
+        launch_pdl(fast::radon_orbit_rows<SO>, rgrid, dim3(256), st, sino, d, rows4,
+                   (int64_t)z0, skip);
+        launch_pdl(fast::radon_bwd_orbit_rows<IO, SPLIT, Epi>, dim3(grid.x, grid.y, zc), block,
+                   st, (const float4*)rows4, static_cast<const float*>(g->ofs), d,
+                   quarter_maps(g), epi, partials ? partials + z0 * per_slice_blocks : nullptr,
+                   skip, (int64_t)z0);
       }
     } else if (g->kind == GR_RADON) {
       fast::radon_bwd_fast<IO, SO, ZB, SPLIT, PY, Epi><<<grid, fblock, 0, st>>>(

@@ -1168,6 +1168,8 @@ template <int IO>
 __global__ void __launch_bounds__(256)
 orbit_pixels(const float* __restrict__ img, Dims d, QuarterMaps qm, float4* __restrict__ img4,
              int64_t z0, const int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t y = blockIdx.y;
@@ -1474,6 +1476,8 @@ fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
               const float* __restrict__ sdpd, FanGeo<float> gg, Dims d, QuarterMaps qm, Epi epi,
               double* __restrict__ partials, const int* __restrict__ skip, int64_t z0) {
   __shared__ double red[32];
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const double part = fan_bwd_orbit_tile<IO, SO, G, Epi>(sino, ofs, sdpd, gg, d, qm, epi,
                                                          blockIdx, z0 + blockIdx.z);
@@ -1825,6 +1829,8 @@ radon_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4
                   Epi epi, double* __restrict__ partials, const int* __restrict__ skip,
                   int64_t z) {
   __shared__ double red[32];
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const double part = radon_fwd_quarter_tile<SO, IO, SPLIT, PIX4, ZS, Epi>(
       img, img4, ofs, g, d, qm, epi, blockIdx, z);
@@ -1847,6 +1853,8 @@ template <int SO>
 __global__ void __launch_bounds__(256)
 radon_orbit_rows(const float* __restrict__ sino, Dims d, float4* __restrict__ rows4, int64_t z0,
                  const int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = blockIdx.y;
@@ -1985,6 +1993,8 @@ radon_bwd_orbit_rows(const float4* __restrict__ rows4, const float* __restrict__
                      QuarterMaps qm, Epi epi, double* __restrict__ partials,
                      const int* __restrict__ skip, int64_t z0) {
   __shared__ double red[32];
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const int64_t nrow = d.Ns + kOrbitRowPad;
   const double part = radon_bwd_orbit_tile<IO, ORDER_F, G, true, Epi>(
@@ -2003,6 +2013,8 @@ radon_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs, D
                 QuarterMaps qm, Epi epi, double* __restrict__ partials,
                 const int* __restrict__ skip, int64_t z0) {
   __shared__ double red[32];
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const double part = radon_bwd_orbit_tile<IO, SO, G, false, Epi>(nullptr, sino, ofs, d, qm, epi,
                                                                   blockIdx, z0 + blockIdx.z);

@@ -125,6 +125,8 @@ __global__ void __launch_bounds__(kSumThreads)
 cg_alpha_kernel(double* sc, const double* __restrict__ partials, int64_t n, double c,
                 const int* skip) {
   __shared__ double red[kSumThreads / 32];
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const double qwq = sum_partials_block(partials, n, red);
   if (threadIdx.x == 0) {
@@ -138,6 +140,8 @@ __global__ void __launch_bounds__(kDotThreads)
 cg_update_d_kernel(T* __restrict__ d, const T* __restrict__ q, const double* __restrict__ sc,
                    double* __restrict__ partials, int64_t n, const int* skip) {
   __shared__ double red[kDotThreads / 32];
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const T na = -(T)sc[GR_SC_ALPHA];
   double acc = 0.0;
@@ -156,6 +160,8 @@ __global__ void __launch_bounds__(kSumThreads)
 cg_beta_kernel(double* sc, const double* __restrict__ snew_partials, int64_t n_snew,
                const double* __restrict__ d_partials, int64_t n_d, double epsilon, int* done) {
   __shared__ double red[kSumThreads / 32];
+  pdl_wait();
+  pdl_trigger();
   if (done != nullptr && *done) return;
   const double snew = sum_partials_block(snew_partials, n_snew, red);
   __syncthreads();
@@ -174,6 +180,8 @@ cg_beta_kernel(double* sc, const double* __restrict__ snew_partials, int64_t n_s
 template <typename T>
 __global__ void cg_update_p_kernel(T* p, const T* __restrict__ snew, const double* __restrict__ sc,
                                    int64_t n, const int* skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip != nullptr && *skip) return;
   const T beta = (T)sc[GR_SC_BETA];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -313,9 +321,11 @@ int gr_cg_alpha(double* sc, const double* partials, size_t n, double c, int dtyp
   if (!sc || !partials || !valid_dtype(dtype)) return GR_ERR_ARG;
   cudaStream_t st = as_stream(stream);
   if (dtype == GR_F32)
-    cg_alpha_kernel<float><<<1, kSumThreads, 0, st>>>(sc, partials, (int64_t)n, c, skip);
+    launch_pdl(cg_alpha_kernel<float>, dim3(1), dim3(kSumThreads), st, sc, partials, (int64_t)n,
+               c, skip);
   else
-    cg_alpha_kernel<double><<<1, kSumThreads, 0, st>>>(sc, partials, (int64_t)n, c, skip);
+    launch_pdl(cg_alpha_kernel<double>, dim3(1), dim3(kSumThreads), st, sc, partials, (int64_t)n,
+               c, skip);
   return check_launch();
 }
 
@@ -324,11 +334,11 @@ int gr_cg_update_d(void* d, const void* q, const double* sc, double* partials, i
   if (!d || !q || !sc || !partials || !valid_dtype(dtype)) return GR_ERR_ARG;
   cudaStream_t st = as_stream(stream);
   if (dtype == GR_F32)
-    cg_update_d_kernel<float><<<kDotBlocks, kDotThreads, 0, st>>>((float*)d, (const float*)q, sc,
-                                                                  partials, (int64_t)n, skip);
+    launch_pdl(cg_update_d_kernel<float>, dim3(kDotBlocks), dim3(kDotThreads), st, (float*)d,
+               (const float*)q, sc, partials, (int64_t)n, skip);
   else
-    cg_update_d_kernel<double><<<kDotBlocks, kDotThreads, 0, st>>>((double*)d, (const double*)q, sc,
-                                                                   partials, (int64_t)n, skip);
+    launch_pdl(cg_update_d_kernel<double>, dim3(kDotBlocks), dim3(kDotThreads), st, (double*)d,
+               (const double*)q, sc, partials, (int64_t)n, skip);
   return check_launch();
 }
 
@@ -337,11 +347,11 @@ int gr_cg_beta(double* sc, const double* snew_partials, size_t n_snew, const dou
   if (!sc || !snew_partials || !d_partials || !valid_dtype(dtype)) return GR_ERR_ARG;
   cudaStream_t st = as_stream(stream);
   if (dtype == GR_F32)
-    cg_beta_kernel<float><<<1, kSumThreads, 0, st>>>(sc, snew_partials, (int64_t)n_snew, d_partials,
-                                                     (int64_t)n_d, epsilon, done);
+    launch_pdl(cg_beta_kernel<float>, dim3(1), dim3(kSumThreads), st, sc, snew_partials,
+               (int64_t)n_snew, d_partials, (int64_t)n_d, epsilon, done);
   else
-    cg_beta_kernel<double><<<1, kSumThreads, 0, st>>>(sc, snew_partials, (int64_t)n_snew,
-                                                      d_partials, (int64_t)n_d, epsilon, done);
+    launch_pdl(cg_beta_kernel<double>, dim3(1), dim3(kSumThreads), st, sc, snew_partials,
+               (int64_t)n_snew, d_partials, (int64_t)n_d, epsilon, done);
   return check_launch();
 }
 
@@ -350,11 +360,11 @@ int gr_cg_update_p(void* p, const void* snew, const double* sc, int dtype, size_
   if (!p || !snew || !sc || !valid_dtype(dtype)) return GR_ERR_ARG;
   cudaStream_t st = as_stream(stream);
   if (dtype == GR_F32)
-    cg_update_p_kernel<float><<<ew_grid(n), kEwBlock, 0, st>>>((float*)p, (const float*)snew, sc,
-                                                               (int64_t)n, skip);
+    launch_pdl(cg_update_p_kernel<float>, dim3(ew_grid(n)), dim3(kEwBlock), st, (float*)p,
+               (const float*)snew, sc, (int64_t)n, skip);
   else
-    cg_update_p_kernel<double><<<ew_grid(n), kEwBlock, 0, st>>>((double*)p, (const double*)snew,
-                                                                sc, (int64_t)n, skip);
+    launch_pdl(cg_update_p_kernel<double>, dim3(ew_grid(n)), dim3(kEwBlock), st, (double*)p,
+               (const double*)snew, sc, (int64_t)n, skip);
   return check_launch();
 }
 
