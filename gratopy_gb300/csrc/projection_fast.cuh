@@ -1031,7 +1031,7 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
             const float2 ma23 = __fmul2_rn(make_float2(qa.z, qa.w), ra2);
 #pragma unroll
             for (int q = 0; q < kRayGroup; ++q) {
-              const float wa = fmaxf(0.0f, 1.0f - fabsf((float)q - ua));
+              const float wa = hat_weight(ua - (float)q);
               const float2 wa2 = make_float2(wa, wa);
               acc01[q] = __ffma2_rn(wa2, a01, acc01[q]);
               acc23[q] = __ffma2_rn(wa2, a23, acc23[q]);
@@ -1069,8 +1069,8 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
           }
 #pragma unroll
           for (int q = 0; q < kRayGroup; ++q) {
-            const float wa = fmaxf(0.0f, 1.0f - fabsf((float)q - ua));
-            const float wb = fmaxf(0.0f, 1.0f - fabsf((float)q - ub));
+            const float wa = hat_weight(ua - (float)q);
+            const float wb = hat_weight(ub - (float)q);
             const float2 wa2 = make_float2(wa, wa), wb2 = make_float2(wb, wb);
             acc01[q] = __ffma2_rn(wb2, b01, __ffma2_rn(wa2, a01, acc01[q]));
             acc23[q] = __ffma2_rn(wb2, b23, __ffma2_rn(wa2, a23, acc23[q]));
@@ -1094,7 +1094,7 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
         // multiply-add of a zero weight leaves the sum unchanged, so no branch
 #pragma unroll
         for (int q = 0; q < kRayGroup; ++q) {
-          const float w = fmaxf(0.0f, 1.0f - fabsf((float)q - u));
+          const float w = hat_weight(u - (float)q);
           const float2 w2 = make_float2(w, w);
           acc01[q] = __ffma2_rn(w2, v01, acc01[q]);
           acc23[q] = __ffma2_rn(w2, v23, acc23[q]);
