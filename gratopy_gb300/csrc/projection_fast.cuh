@@ -2024,11 +2024,15 @@ radon_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs, D
   }
 }
 
-// (The mirrored kernel with two candidates per trip at 94 registers, capped
-// at 80 for 6 blocks per SM, spilled and ran 512^2 x 360 in 99.4 instead of
-// 77.0 us.)
+// The mirrored kernel with 32 lanes per bin group (the form the projections
+// launch) is held to 72 registers, 7 blocks per SM instead of 6 at its
+// natural 80 (one 4-byte spill): 512^2 x 360 forward 1471-1473 -> 1516-1534
+// Gpixel-angle/s, and the 2048^2 x 64 TV iteration 323.1 -> 314.5 ms.  At 64
+// registers (8 blocks) it spills 80 bytes.  (Two candidates per trip took 94
+// registers, and capped at 80 for 6 blocks per SM spilled and ran 512^2 x
+// 360 in 99.4 instead of 77.0 us.)
 template <int SO, int IO, int SPLIT, bool PIX4, bool MIRROR, class Epi>
-__global__ void __launch_bounds__(kFwdBlock)
+__global__ void __launch_bounds__(kFwdBlock, MIRROR && SPLIT >= 32 ? 7 : 1)
 fan_fwd_quarter(const float* __restrict__ img, const float4* __restrict__ img4,
                 const float* __restrict__ ofs,
                 const float* __restrict__ sdpd, FanGeo<float> g, Dims d, QuarterMaps qm, Epi epi,
