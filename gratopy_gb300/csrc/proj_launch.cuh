@@ -208,6 +208,28 @@ inline bool use_quarter_bwd(const gr_geometry* g, int Nz) {
   return maps_cyclic(g);
 }
 
+// Registers of the fan-beam orbit backprojection (fan_bwd_orbit_rows).  With
+// 8 angle groups and slices of at most 512^2 pixels it runs 5 blocks per SM
+// at 48 registers instead of 4 at 64 (8-20 bytes of spill): 512^2 x 360
+// backprojection 1618 -> 1676-1704 Gpixel-angle/s, CG-50 112.2 -> 115.0
+// reconstructions/s.  The TV epilogues keep 4 blocks: at 48 registers their
+// F-ordered form spills 40 bytes, and the 2048^2 x 64 TV iteration took
+// 349.8 instead of 314.6 ms.  Larger slices keep 4 blocks as well (that
+// iteration is the only measurement above 512^2).
+template <class Epi>
+struct tv_epilogue : std::false_type {};
+template <typename T, int O>
+struct tv_epilogue<BwdTVPrimal<T, O>> : std::true_type {};
+template <typename T, int O>
+struct tv_epilogue<BwdTVAdjoint<T, O>> : std::true_type {};
+template <class Epi, int G>
+constexpr int kDenseFanBwdBlocks = (G == 8 && !tv_epilogue<Epi>::value) ? 5 : 1;
+constexpr int64_t kDenseFanBwdMaxPixels = 512 * 512;
+template <class Epi, int G>
+inline bool dense_fan_bwd(const gr_geometry* g) {
+  return kDenseFanBwdBlocks<Epi, G> > 1 && (int64_t)g->Nx * g->Ny <= kDenseFanBwdMaxPixels;
+}
+
 // Scratch of the orbit kernels: the forward's orbit pixels (one float4 per
 // pixel) and the backprojection's interleaved rows (one float4 per base
 // angle and bin); one call uses one of them, so the larger one is needed.
@@ -595,7 +617,10 @@ int launch_bwd_zb(const gr_geometry* g, const T* sino, int Nz, Epi epi, double* 
           const dim3 rgrid((g->Ns + fast::kOrbitRowPad + 255) / 256 + 1, g->Na / 4, zc);
           launch_pdl(fast::orbit_rows<SO>, rgrid, dim3(256), st, sino, sdpd, ofs,
                      fan_geo<float>(g->geo), d, rows4, (int64_t)z0, skip);
-          launch_pdl(fast::fan_bwd_orbit_rows<IO, SPLIT, Epi>, dim3(grid.x, grid.y, zc), block, st,
+          auto* kernel = dense_fan_bwd<Epi, SPLIT>(g)
+                             ? fast::fan_bwd_orbit_rows<IO, SPLIT, kDenseFanBwdBlocks<Epi, SPLIT>, Epi>
+                             : fast::fan_bwd_orbit_rows<IO, SPLIT, 1, Epi>;
+          launch_pdl(kernel, dim3(grid.x, grid.y, zc), block, st,
                      (const float4*)rows4, fan_geo<float>(g->geo), d, quarter_maps(g), epi,
                      partials ? partials + z0 * per_slice_blocks : nullptr, skip, (int64_t)z0);
         }

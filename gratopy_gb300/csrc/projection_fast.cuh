@@ -1511,8 +1511,12 @@ fan_bwd_orbit(const float* __restrict__ sino, const float* __restrict__ ofs,
 // copy, the quadrant's pixels x <= y -- measured slower: 512^2 x 360 77.2
 // against 68.2 us, 2048^2 x 1440 3001 against 2620 us; the same L1 bytes per
 // pixel-angle from half the threads, each with twice the footprint.)
-template <int IO, int G, class Epi>
-__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow)
+//
+// MINB: the minimum resident blocks per SM the registers are fitted to (1:
+// the compiler's choice, 64 registers; 5: 48 registers, which the launch
+// picks where it measured faster).
+template <int IO, int G, int MINB, class Epi>
+__global__ void __launch_bounds__(kBwdTileFast * kBwdTileSlow, MINB)
 fan_bwd_orbit_rows(const float4* __restrict__ rows4, FanGeo<float> gg, Dims d, QuarterMaps qm,
                    Epi epi, double* __restrict__ partials, const int* __restrict__ skip,
                    int64_t z0) {
