@@ -1016,9 +1016,10 @@ __device__ __forceinline__ double fan_fwd_quarter_tile(const float* __restrict__
         // per trip.
         if constexpr (MIRROR) {
           // one candidate per trip: its two loads (P and M P) in flight and
-          // 80 registers instead of 94 (two per trip: 512^2 x 360 equal,
-          // 1024^2 x 720 387.5 against 382.2 us, 2048^2 x 1440 2618
-          // against 2592 us); the same sums bit for bit
+          // 80 registers unbounded instead of 94 (two per trip: 512^2 x 360
+          // equal, 1024^2 x 720 387.5 against 382.2 us, 2048^2 x 1440 2618
+          // against 2592 us); the same sums bit for bit.  The kernel's
+          // launch bounds now hold the 32-lane form to 72.
           for (int x = xlo; x <= xhi; ++x) {
             const float4 pa = __ldg(img4 + o0);
             const float4 qa = __ldg(img4 + oM);
